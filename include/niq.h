@@ -1,0 +1,222 @@
+/*
+ * niq.h -- C ABI of the GB300 range-analysis query engine (libniq.so).
+ *
+ * Drop-in boundary for the range-analysis hot path of nmwsharp/neural-implicit-queries.
+ * The reference is pure Python/JAX and has no FFI of its own; each entry point below
+ * replaces one reference function (cited as src/<file>:<line> inside that project).
+ * A Python host layer re-exposes the reference's names and signatures on top of it.
+ *
+ * Conventions
+ *  - Every function returns an int status: NIQ_OK (0) or a negative NIQ_ERR_* code;
+ *    niq_last_error() gives a one-line message for the calling thread.
+ *  - All array arguments are DEVICE pointers owned by the caller (float32, int32 or
+ *    int64 as typed), row-major; points and box centers are (n, 3).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Calls
+ *    are asynchronous on that stream unless documented otherwise ("syncs").
+ *  - Scratch memory is caller-provided (`workspace`, `workspace_bytes`); each query has a
+ *    *_workspace_size() helper.  A workspace too small for the work found at run time
+ *    returns NIQ_ERR_CAPACITY and leaves outputs undefined.
+ *  - A model handle is immutable after niq_model_create and may be shared by streams;
+ *    one workspace must not be used by two calls in flight at once.
+ */
+#ifndef NIQ_H
+#define NIQ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define NIQ_OK                 0
+#define NIQ_ERR_INVALID_ARG   -1  /* bad pointer, size or option                      */
+#define NIQ_ERR_BAD_SPEC      -2  /* packed spec malformed (src/mlp.py:131,142)       */
+#define NIQ_ERR_CUDA          -3  /* CUDA runtime error                               */
+#define NIQ_ERR_CAPACITY      -4  /* workspace / output capacity exceeded             */
+#define NIQ_ERR_TIMEOUT       -5  /* a bounded device-side wait gave up               */
+#define NIQ_ERR_UNSUPPORTED   -6  /* mode / width / depth outside the built kernels   */
+
+/* ---- sign codes: src/implicit_function.py:11-13 --------------------------------- */
+#define NIQ_SIGN_UNKNOWN   0
+#define NIQ_SIGN_POSITIVE  1
+#define NIQ_SIGN_NEGATIVE  2
+
+/* ---- range-arithmetic modes: src/implicit_mlp_utils.py:12-64, src/affine.py:62-76 -- */
+#define NIQ_MODE_INTERVAL         0
+#define NIQ_MODE_AFFINE_FIXED     1
+#define NIQ_MODE_AFFINE_TRUNCATE  2
+#define NIQ_MODE_AFFINE_APPEND    3
+#define NIQ_MODE_AFFINE_ALL       4
+#define NIQ_MODE_SLOPE_INTERVAL   5
+
+/* ---- activation codes inside a packed spec ---------------------------------------- */
+#define NIQ_ACT_NONE  0
+#define NIQ_ACT_RELU  1   /* src/affine_layers.py:34-56   */
+#define NIQ_ACT_ELU   2   /* src/affine_layers.py:59-97   */
+#define NIQ_ACT_TANH  3   /* no reference rule: new        */
+
+#define NIQ_MAX_LAYERS 32
+#define NIQ_MAX_WIDTH  256
+#define NIQ_SPEC_MAGIC 0x3151494eu /* "NIQ1" */
+
+typedef struct niq_model niq_model;
+
+/* Options of one range-analysis evaluation (the reference's AffineContext,
+ * src/affine.py:62-76).  truncate_count is used by AFFINE_TRUNCATE, n_append by
+ * AFFINE_APPEND.  conservative != 0 adds the outward rounding-error terms. */
+typedef struct niq_bound_opts {
+    int32_t mode;
+    int32_t truncate_count;
+    int32_t n_append;
+    int32_t conservative;
+} niq_bound_opts;
+
+/* The cast options dict of src/queries.py:23-36. */
+typedef struct niq_cast_opts {
+    float   hit_eps;
+    float   max_dist;
+    int32_t n_max_step;
+    int32_t n_substeps;
+    float   safety_factor;
+    float   interval_grow_fac;
+    float   interval_shrink_fac;
+    float   interval_init_size;
+} niq_cast_opts;
+
+/* ---- library ---------------------------------------------------------------------- */
+const char* niq_last_error(void);
+int niq_version(void);
+/* Number of SMs and resident-CTA counts of the current device (for workspace sizing). */
+int niq_device_info(int32_t* sm_count, int32_t* max_smem_per_block);
+
+/* ---- models: the dict spec of src/mlp.py:14-24,117-144 packed by the host layer ---- */
+/* Validates and uploads a packed spec (host memory) to the current device.
+ * Replaces the trace-time spec walk of src/mlp.py:96-113 (func_from_spec/eval_spec). */
+int niq_model_create(const void* packed_spec, size_t bytes, niq_model** out);
+int niq_model_destroy(niq_model* model);
+/* Widest layer and number of dense layers of a model. */
+int niq_model_info(const niq_model* model, int32_t* max_width, int32_t* n_layers);
+
+/* ---- point evaluation: ImplicitFunction.__call__ (src/affine.py:26-28,
+ *      src/mlp.py:253-347) --------------------------------------------------------- */
+int niq_eval_points(const niq_model* model, int64_t n, const float* xyz, float* out,
+                    void* stream);
+
+/* ---- range bounds: classify_general_box (src/affine.py:34-55,
+ *      src/slope_interval.py:29-51).  center (n,3), vecs (n,v,3) with 1 <= v <= 3.
+ *      sign_out (n) gets NIQ_SIGN_*, lo_hi_out (n,2) optional (may be NULL).
+ *      Growing-term modes (TRUNCATE/APPEND/ALL) need a workspace of
+ *      niq_classify_workspace_size() bytes; the fixed modes accept NULL. ---------- */
+size_t niq_classify_workspace_size(const niq_model* model, const niq_bound_opts* opts,
+                                   int64_t n, int32_t v);
+int niq_classify_boxes(const niq_model* model, const niq_bound_opts* opts, int64_t n,
+                       const float* center, const float* vecs, int32_t v, float offset,
+                       int32_t* sign_out, float* lo_hi_out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- ray casting: queries.cast_rays (src/queries.py:39-175) ------------------------ *
+ * models[nfunc] are the functions of funcs_tuple; hit_id is 1-based (0 = no hit).
+ * Persistent kernel: every ray steps on the device until it terminates; no host
+ * round trip per iteration.  n_evals_out (device int64) counts ray-steps evaluated
+ * per function.  workspace: niq_cast_rays_workspace_size() bytes. */
+size_t niq_cast_rays_workspace_size(int32_t nfunc, int64_t n);
+int niq_cast_rays(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
+                  int64_t n, const float* roots, const float* dirs, const niq_cast_opts* cast,
+                  float* t_out, int32_t* hit_id_out, int32_t* count_out, int64_t* n_evals_out,
+                  void* workspace, size_t workspace_bytes, void* stream);
+/* The plain form: one launch per iteration over the live rays with a host-side
+ * compaction step between iterations, the structure of the reference's loop
+ * (src/queries.py:158-173).  Syncs the stream. */
+int niq_cast_rays_plain(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
+                        int64_t n, const float* roots, const float* dirs, const niq_cast_opts* cast,
+                        float* t_out, int32_t* hit_id_out, int32_t* count_out, int64_t* n_evals_out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- level-set kd-tree: construct_uniform_unknown_levelset_tree
+ *      (src/kd_tree.py:19-218) ------------------------------------------------------ *
+ * Breadth-first bisection of the box [lower, upper] (host float[3] each) for
+ * split_depth+1 classify rounds (split_depth < 0: none) or until a round starts with
+ * >= node_terminate_thresh nodes (<= 0: none).  Results land in the workspace; the
+ * counts are written to the device int64 array counts_out[4] =
+ * {n_unknown, n_interior, n_exterior, n_boxes_classified} and the node arrays are read
+ * back with niq_tree_result().  flags: bit0 with_interior_nodes, bit1
+ * with_exterior_nodes.  Persistent cooperative kernel, one launch for all levels. */
+#define NIQ_TREE_WITH_INTERIOR 1
+#define NIQ_TREE_WITH_EXTERIOR 2
+size_t niq_tree_workspace_size(int64_t node_capacity, int32_t flags);
+int niq_levelset_tree(const niq_model* model, const niq_bound_opts* opts,
+                      const float* lower, const float* upper, int32_t split_depth,
+                      int64_t node_terminate_thresh, float offset, int32_t flags,
+                      int64_t node_capacity, int64_t* counts_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+/* The plain form: one launch + host sync per level (src/kd_tree.py:137-198). */
+int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts,
+                            const float* lower, const float* upper, int32_t split_depth,
+                            int64_t node_terminate_thresh, float offset, int32_t flags,
+                            int64_t node_capacity, int64_t* counts_out,
+                            void* workspace, size_t workspace_bytes, void* stream);
+/* Device pointers into a finished tree workspace: kind 0 unknown, 1 interior,
+ * 2 exterior; lower/upper are (node_capacity, 3) arrays whose first count rows hold
+ * the result. */
+int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32_t kind,
+                    float** lower, float** upper);
+
+/* ---- hierarchical marching cubes: hierarchical_marching_cubes
+ *      (src/kd_tree.py:338-399, src/extract_cell.py:306-421) ------------------------ *
+ * Extracts triangles (n_tris_out[0] of them, <= tri_capacity) from the n_leaves
+ * boxes (lower/upper (n_leaves,3), e.g. niq_tree_result kind 0) on a
+ * (2^n_subcell_depth)^3 subgrid each.  tris_out is (tri_capacity, 3, 3). */
+int niq_hmc_extract(const niq_model* model, int64_t n_leaves, const float* leaf_lower,
+                    const float* leaf_upper, int32_t n_subcell_depth,
+                    float* tris_out, int64_t tri_capacity, int64_t* n_tris_out, void* stream);
+
+/* ---- pairwise intersection: find_any_intersection (src/kd_tree.py:402-655) ---------- *
+ * found_out (device int32[1]) = 1 when an intersection is found, loc_out (device
+ * float[3]) its witness, (-777,-777,-777) otherwise.  Persistent kernel over all depths;
+ * counts_out (device int64[2]) = {nodes processed, depth reached}. */
+size_t niq_intersect_workspace_size(int64_t node_capacity);
+int niq_find_any_intersection(const niq_model* model_a, const niq_model* model_b,
+                              const niq_bound_opts* opts, const float* lower, const float* upper,
+                              float eps, int64_t node_capacity, int32_t* found_out, float* loc_out,
+                              int64_t* counts_out, void* workspace, size_t workspace_bytes,
+                              void* stream);
+
+/* ---- closest point: closest_point (src/kd_tree.py:659-802) -------------------------- *
+ * The reference schedule: one global LIFO stack, batch pops of batch_process_size
+ * nodes, scatter-min of candidate distances.  Host loop with one sync per batch. */
+size_t niq_closest_point_workspace_size(int64_t n_queries, int32_t batch_process_size,
+                                        int64_t stack_capacity);
+int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                      const float* upper, int64_t n_queries, const float* query_points,
+                      float eps, int32_t batch_process_size, int64_t stack_capacity,
+                      float* min_dist_out, float* min_loc_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+/* Persistent form: every query traverses its own depth-first stack on the device,
+ * nearer child first; one launch.  Same candidate and pruning tests as the reference;
+ * the visiting order differs, see the design doc for the resulting tolerance. */
+size_t niq_closest_point_persistent_workspace_size(int64_t n_queries);
+int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* opts,
+                                 const float* lower, const float* upper, int64_t n_queries,
+                                 const float* query_points, float eps,
+                                 float* min_dist_out, float* min_loc_out,
+                                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- many models in one launch (closest point over a model table) ------------------ *
+ * Job j runs query_count[j] closest-point queries starting at row query_offset[j] of
+ * query_points against models[job_model[j]]; all jobs run in one persistent launch.
+ * Arrays job_model/query_offset/query_count are host arrays of n_jobs entries. */
+size_t niq_batched_closest_point_workspace_size(int64_t total_queries, int32_t n_jobs);
+int niq_batched_closest_point(const niq_model* const* models, int32_t n_models,
+                              const niq_bound_opts* opts, int32_t n_jobs,
+                              const int32_t* job_model, const int64_t* query_offset,
+                              const int64_t* query_count, const float* query_points,
+                              const float* lower, const float* upper, float eps,
+                              float* min_dist_out, float* min_loc_out,
+                              void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NIQ_H */

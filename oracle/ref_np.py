@@ -1,0 +1,800 @@
+"""CPU restatement (NumPy) of the range-analysis hot path of nmwsharp/neural-implicit-queries.
+
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: it is imported by ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` and nowhere else.
+The product path (the CUDA kernels behind ``include/niq.h``) never calls it.
+
+Every function restates one reference function, vectorised over a leading batch axis
+(where the reference uses ``jax.vmap``) and parameterised by ``dtype``:
+``np.float32`` mirrors the reference's fp32 JAX arithmetic, ``np.float64`` is the
+FP64 affine-arithmetic oracle used to judge bound widths.
+
+Parity pin: ``tests/golden/make_golden.py`` executes the reference's own ``src/*.py``
+(over a NumPy stand-in for the absent ``jax`` package) on seeded inputs and commits the
+outputs under ``tests/golden/``; ``tests/test_oracle_golden.py`` checks this module
+against them.  The stand-in replaces XLA's arithmetic, so the pin holds within fp32
+rounding, not bit for bit.
+
+Citations are ``path:line`` inside the reference project.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SIGN_UNKNOWN = 0   # src/implicit_function.py:11
+SIGN_POSITIVE = 1  # src/implicit_function.py:12
+SIGN_NEGATIVE = 2  # src/implicit_function.py:13
+
+AFFINE_MODES = ('interval', 'affine_fixed', 'affine_truncate', 'affine_append', 'affine_all')
+
+
+# ----------------------------------------------------------------------------------------
+# Spec walking  (src/mlp.py:117-144)
+# ----------------------------------------------------------------------------------------
+
+def n_ops(params):
+    """src/mlp.py:135-144: one past the largest 4-digit op prefix."""
+    n = 0
+    for key in params:
+        try:
+            i_op = int(key.split(".")[0])
+        except ValueError:
+            raise ValueError(f"Could not parse out key {key}. Is this a valid mlp spec?")
+        n = max(n, i_op + 1)
+    return n
+
+
+def get_op_data(params, i_op):
+    """src/mlp.py:117-133: (name, {arg: value}) of op ``i_op``; the ``_`` arg is dropped
+    later by the evaluator (src/mlp.py:108-109)."""
+    prefix = f"{i_op:04d}"
+    name, args = "", {}
+    for key in params:
+        if key.startswith(prefix):
+            tokens = key.split(".")
+            name = tokens[1]
+            if len(tokens) > 2:
+                args[tokens[2]] = params[key]
+    if name == "":
+        raise ValueError(f"didn't find op {i_op}")
+    args.pop("_", None)
+    return name, args
+
+
+def spec_ops(params, dtype=np.float32):
+    """Ops in order with their arrays cast to ``dtype``.  ``spatial_transformation`` is
+    rewritten into the dense op it applies: ``x @ inv(R) + inv(R) @ (-t)``
+    (src/mlp.py:342-346, src/affine_layers.py:175-179)."""
+    ops = []
+    for i in range(n_ops(params)):
+        name, args = get_op_data(params, i)
+        if name == 'dense':
+            A = np.asarray(args['A'], dtype=dtype)
+            b = args.get('b', None)
+            b = None if b is None else np.asarray(b, dtype=dtype)
+            ops.append(('dense', A, b))
+        elif name == 'spatial_transformation':
+            R = np.asarray(args['R'], dtype=dtype)
+            t = np.asarray(args['t'], dtype=dtype)
+            R_inv = np.linalg.inv(R).astype(dtype)
+            t_inv = (R_inv @ (-t)).astype(dtype)
+            ops.append(('dense', R_inv, t_inv))
+        elif name in ('relu', 'elu', 'tanh', 'squeeze_last'):
+            ops.append((name,))
+        else:
+            raise ValueError(f"unsupported op '{name}'")
+    return ops
+
+
+# ----------------------------------------------------------------------------------------
+# Point evaluation  (src/mlp.py:253-347, const paths of src/affine_layers.py)
+# ----------------------------------------------------------------------------------------
+
+def _elu(x):
+    # jax.nn.elu: where(x > 0, x, expm1(where(x > 0, 0, x)))
+    return np.where(x > 0, x, np.expm1(np.where(x > 0, 0, x)))
+
+
+def eval_points(params, x, dtype=np.float32):
+    """Plain MLP forward for points ``x`` of shape (N, 3) -> (N,)."""
+    x = np.asarray(x, dtype=dtype)
+    for op in spec_ops(params, dtype):
+        name = op[0]
+        if name == 'dense':
+            _, A, b = op
+            x = x @ A
+            if b is not None:
+                x = x + b
+        elif name == 'relu':
+            x = np.maximum(x, 0)
+        elif name == 'elu':
+            x = _elu(x)
+        elif name == 'tanh':
+            x = np.tanh(x)
+        elif name == 'squeeze_last':
+            x = x[..., 0]
+    return x
+
+
+# ----------------------------------------------------------------------------------------
+# Affine arithmetic  (src/affine.py, src/affine_layers.py)
+# ----------------------------------------------------------------------------------------
+
+@dataclass(frozen=True)
+class AffineContext:
+    """src/affine.py:62-76."""
+    mode: str = 'affine_fixed'
+    truncate_count: int = -777
+    truncate_policy: str = 'absolute'
+    affine_domain_terms: int = 0
+    n_append: int = 0
+
+    def __post_init__(self):
+        if self.mode not in AFFINE_MODES:
+            raise ValueError("invalid mode")
+        if self.mode == 'affine_truncate' and self.truncate_count is None:
+            raise ValueError("must specify truncate count")
+
+
+def coordinates_in_general_box(ctx, center, vecs):
+    """src/affine.py:109-117, batched: center (N,d), vecs (N,v,d)."""
+    base = center
+    if ctx.mode == 'interval':
+        aff = np.zeros((center.shape[0], 0, center.shape[-1]), dtype=center.dtype)
+        err = np.sum(np.abs(vecs), axis=1)
+    else:
+        aff = vecs
+        err = np.zeros_like(center)
+    return base, aff, err
+
+
+def radius(aff, err):
+    """src/affine.py:85-91."""
+    return np.sum(np.abs(aff), axis=1) + err
+
+
+def may_contain_bounds(base, aff, err):
+    """src/affine.py:119-125."""
+    rad = radius(aff, err)
+    return base - rad, base + rad
+
+
+def truncate_affine(ctx, base, aff, err):
+    """src/affine.py:127-162 ('absolute' policy; rows sorted by decreasing L1 magnitude,
+    stable, the first ``truncate_count`` kept, the rest folded into ``err``)."""
+    if ctx.mode != 'affine_truncate':
+        return base, aff, err
+    n_keep = ctx.truncate_count
+    if aff.shape[1] <= n_keep:
+        return base, aff, err
+    if ctx.truncate_policy != 'absolute':
+        raise RuntimeError("bad policy")
+    mags = np.sum(np.abs(aff), axis=-1)                      # (N, rows)
+    order = np.argsort(-mags, axis=-1, kind='stable')        # jnp.argsort is stable
+    aff = np.take_along_axis(aff, order[:, :, None], axis=1)
+    err = err + np.sum(np.abs(aff[:, n_keep:, :]), axis=1)
+    return base, aff[:, :n_keep, :], err
+
+
+def apply_linear_approx(ctx, base, aff, err, alpha, beta, delta):
+    """src/affine.py:164-193."""
+    base = alpha * base + beta
+    aff = alpha[:, None, :] * aff
+    delta = np.abs(delta)
+    if ctx.mode in ('interval', 'affine_fixed'):
+        err = alpha * err + delta
+    elif ctx.mode in ('affine_truncate', 'affine_all'):
+        err = alpha * err
+        n, d = delta.shape
+        new_aff = np.zeros((n, d, d), dtype=delta.dtype)
+        new_aff[:, np.arange(d), np.arange(d)] = delta
+        aff = np.concatenate((aff, new_aff), axis=1)
+        base, aff, err = truncate_affine(ctx, base, aff, err)
+    elif ctx.mode == 'affine_append':
+        err = alpha * err
+        k = ctx.n_append
+        # jax.lax.top_k: descending, ties to the lower index
+        order = np.argsort(-delta, axis=-1, kind='stable')[:, :k]
+        keep_vals = np.take_along_axis(delta, order, axis=-1)
+        n, d = delta.shape
+        new_aff = np.zeros((n, k, d), dtype=delta.dtype)
+        new_aff[np.arange(n)[:, None], np.arange(k)[None, :], order] = keep_vals
+        aff = np.concatenate((aff, new_aff), axis=1)
+        err = err + (np.sum(delta, axis=-1) - np.sum(keep_vals, axis=-1))[:, None]
+    return base, aff, err
+
+
+def _relu_linearization(lower, upper):
+    """src/affine_layers.py:34-56 (Chebyshev bound of relu on [lower, upper])."""
+    relu = lambda v: np.maximum(v, 0)
+    with np.errstate(divide='ignore', invalid='ignore', over='ignore'):
+        alpha = (relu(upper) - relu(lower)) / (upper - lower)
+    alpha = np.where(lower >= 0, 1., alpha)
+    alpha = np.where(upper < 0, 0., alpha)
+    alpha = np.nan_to_num(alpha, nan=0.0)
+    alpha = np.clip(alpha, 0., 1.)
+    beta = (relu(lower) - alpha * lower) / 2
+    delta = beta
+    return alpha.astype(lower.dtype), beta.astype(lower.dtype), delta.astype(lower.dtype)
+
+
+def _elu_linearization(lower, upper):
+    """src/affine_layers.py:59-97."""
+    with np.errstate(divide='ignore', invalid='ignore', over='ignore'):
+        lowerF = _elu(lower)
+        upperF = _elu(upper)
+        lowerS = np.minimum(np.exp(lower), 1.)
+        upperS = np.minimum(np.exp(upper), 1.)
+        alpha = (upperF - lowerF) / (upper - lower)
+        alpha = np.where(lower >= 0, 1., alpha)
+        alpha = np.nan_to_num(alpha, nan=0.0)
+        alpha = np.clip(alpha, lowerS, upperS)
+        r_upper = lowerF - alpha * lower
+        x_lower = np.clip(np.log(alpha), lower, upper)
+        r_lower = (alpha - 1.) - alpha * x_lower
+    beta = 0.5 * (r_upper + r_lower)
+    delta = 0.5 * np.abs(r_upper - r_lower)
+    alpha = np.where(lower >= 0, 1., alpha)
+    beta = np.where(lower >= 0, 0., beta)
+    delta = np.where(lower >= 0, 0., delta)
+    dt = lower.dtype
+    return alpha.astype(dt), beta.astype(dt), delta.astype(dt)
+
+
+def _tanh_linearization(lower, upper):
+    """TanH has no rule in the reference (its README names TanH, the code has none).
+    This rule follows the pattern of the reference's ``sin``/``elu`` rules
+    (src/affine_layers.py:59-138): the secant slope ``alpha`` on [lower, upper]; the
+    extrema of ``tanh(x) - alpha*x`` are taken over the endpoints and the interior
+    stationary points ``x = +-atanh(sqrt(1 - alpha))`` clipped into the interval;
+    ``beta`` is their midpoint and ``delta`` their half-range."""
+    dt = lower.dtype
+    with np.errstate(divide='ignore', invalid='ignore', over='ignore'):
+        tl, tu = np.tanh(lower), np.tanh(upper)
+        width = upper - lower
+        alpha = (tu - tl) / width
+        mid = 0.5 * (lower + upper)
+        tm = np.tanh(mid)
+        alpha = np.where(width > 0, alpha, 1. - tm * tm)
+        alpha = np.nan_to_num(alpha, nan=0.0)
+        alpha = np.clip(alpha, 0., 1.)
+        xs = np.arctanh(np.sqrt(np.clip(1. - alpha, 0., 1.)))   # +inf when alpha == 0
+        cands = [lower, upper, np.clip(xs, lower, upper), np.clip(-xs, lower, upper)]
+        vals = [np.tanh(c) - alpha * c for c in cands]
+        r_lo = np.minimum.reduce(vals)
+        r_hi = np.maximum.reduce(vals)
+    beta = 0.5 * (r_hi + r_lo)
+    delta = 0.5 * (r_hi - r_lo)
+    return alpha.astype(dt), beta.astype(dt), delta.astype(dt)
+
+
+_LINEARIZATIONS = {'relu': _relu_linearization, 'elu': _elu_linearization,
+                   'tanh': _tanh_linearization}
+
+
+def affine_forward(params, ctx, base, aff, err, dtype=np.float32):
+    """Walk the spec in affine mode (src/mlp.py:99-111 with apply_func['affine'])."""
+    for op in spec_ops(params, dtype):
+        name = op[0]
+        if name == 'dense':                     # src/affine_layers.py:11-31
+            _, A, b = op
+            base = base @ A
+            aff = aff @ A
+            err = err @ np.abs(A)
+            if b is not None:
+                base = base + b
+        elif name in _LINEARIZATIONS:
+            lower, upper = may_contain_bounds(base, aff, err)
+            alpha, beta, delta = _LINEARIZATIONS[name](lower, upper)
+            base, aff, err = apply_linear_approx(ctx, base, aff, err, alpha, beta, delta)
+        elif name == 'squeeze_last':            # src/affine_layers.py:164-172
+            base, aff, err = base[..., 0], aff[..., 0], err[..., 0]
+    return base, aff, err
+
+
+def affine_bounds(params, ctx, center, vecs, dtype=np.float32):
+    """(lower, upper) of the output over general boxes: center (N,3), vecs (N,v,3)."""
+    center = np.asarray(center, dtype=dtype)
+    vecs = np.asarray(vecs, dtype=dtype)
+    ctx = AffineContext(ctx.mode, ctx.truncate_count, ctx.truncate_policy,
+                        vecs.shape[1], ctx.n_append)
+    base, aff, err = coordinates_in_general_box(ctx, center, vecs)
+    base, aff, err = affine_forward(params, ctx, base, aff, err, dtype)
+    return may_contain_bounds(base, aff, err)
+
+
+def sign_from_bounds(lower, upper, offset=0.):
+    """src/affine.py:50-53 and src/slope_interval.py:44-47."""
+    out = np.full(lower.shape, SIGN_UNKNOWN, dtype=np.int32)
+    out = np.where(lower > offset, SIGN_POSITIVE, out)
+    out = np.where(upper < -offset, SIGN_NEGATIVE, out)
+    return out.astype(np.int32)
+
+
+# ----------------------------------------------------------------------------------------
+# Slope intervals  (src/slope_interval.py, src/slope_interval_layers.py)
+# ----------------------------------------------------------------------------------------
+
+def slope_forward(params, primal, center, width, dtype=np.float32):
+    for op in spec_ops(params, dtype):
+        name = op[0]
+        if name == 'dense':                     # src/slope_interval_layers.py:11-33
+            _, A, b = op
+            primal = primal @ A
+            if b is not None:
+                primal = primal + b
+            center = center @ A
+            width = width @ np.abs(A)
+        elif name in ('relu', 'elu', 'tanh'):   # src/slope_interval_layers.py:36-82
+            sl, su = center - width, center + width
+            rad = np.sum(np.maximum(su, -sl), axis=1)
+            pl, pu = primal - rad, primal + rad
+            if name == 'relu':
+                dfl = np.where(pl > 0, 1., 0.).astype(dtype)
+                dfu = np.where(pu < 0, 0., 1.).astype(dtype)
+                primal = np.maximum(primal, 0)
+            elif name == 'elu':
+                dfl = np.minimum(np.exp(pl), 1.).astype(dtype)
+                dfu = np.minimum(np.exp(pu), 1.).astype(dtype)
+                primal = _elu(primal)
+            else:  # tanh: derivative 1 - tanh^2 is largest at 0, decreasing in |x|
+                dl = 1. - np.tanh(pl) ** 2
+                du = 1. - np.tanh(pu) ** 2
+                straddle = (pl <= 0) & (pu >= 0)
+                dfl = np.minimum(dl, du).astype(dtype)
+                dfu = np.where(straddle, 1., np.maximum(dl, du)).astype(dtype)
+                primal = np.tanh(primal)
+            nl = np.minimum(sl * dfl[:, None, :], sl * dfu[:, None, :])
+            nu = np.maximum(su * dfl[:, None, :], su * dfu[:, None, :])
+            center = 0.5 * (nl + nu)
+            width = nu - center
+        elif name == 'squeeze_last':
+            primal, center, width = primal[..., 0], center[..., 0], width[..., 0]
+    return primal, center, width
+
+
+def slope_bounds_box(params, center, vecs, dtype=np.float32):
+    """src/slope_interval.py:29-51,192-210 batched: returns (lower, upper)."""
+    center = np.asarray(center, dtype=dtype)
+    vecs = np.asarray(vecs, dtype=dtype)
+    primal, sc, sw = slope_forward(params, center, vecs, np.zeros_like(vecs), dtype)
+    sl, su = sc - sw, sc + sw
+    rad = np.sum(np.maximum(su, -sl), axis=1)
+    return primal - rad, primal + rad
+
+
+# ----------------------------------------------------------------------------------------
+# ImplicitFunction-like façade (src/implicit_function.py:28-37, src/implicit_mlp_utils.py)
+# ----------------------------------------------------------------------------------------
+
+@dataclass
+class OracleFunc:
+    """A mode-bound evaluator: ``mode`` is one of the names of
+    src/implicit_mlp_utils.py:12-64 except 'sdf'."""
+    mode: str = 'affine_fixed'
+    truncate_count: int = -777
+    n_append: int = 0
+    dtype: type = np.float32
+    ctx: AffineContext = field(init=False, default=None)
+
+    def __post_init__(self):
+        if self.mode != 'slope_interval':
+            self.ctx = AffineContext(self.mode, truncate_count=self.truncate_count,
+                                     n_append=self.n_append)
+
+    def __call__(self, params, x):
+        return eval_points(params, x, self.dtype)
+
+    def bounds_general(self, params, center, vecs):
+        if self.mode == 'slope_interval':
+            return slope_bounds_box(params, center, vecs, self.dtype)
+        return affine_bounds(params, self.ctx, center, vecs, self.dtype)
+
+    def classify_general_box(self, params, center, vecs, offset=0.):
+        lo, hi = self.bounds_general(params, center, vecs)
+        return sign_from_bounds(lo, hi, offset)
+
+    def classify_box(self, params, lower, upper, offset=0.):
+        lower = np.asarray(lower, self.dtype)
+        upper = np.asarray(upper, self.dtype)
+        center = 0.5 * (lower + upper)
+        vec = upper - center
+        vecs = np.zeros(vec.shape[:1] + (3, 3), dtype=self.dtype)
+        vecs[:, np.arange(3), np.arange(3)] = vec
+        return self.classify_general_box(params, center, vecs, offset)
+
+
+def generate_implicit(params, mode, **kwargs):
+    """src/implicit_mlp_utils.py:12-64 without the file load."""
+    if mode == 'affine_truncate':
+        f = OracleFunc(mode, truncate_count=kwargs['affine_n_truncate'])
+    elif mode == 'affine_append':
+        f = OracleFunc(mode, n_append=kwargs['affine_n_append'])
+    elif mode in AFFINE_MODES or mode == 'slope_interval':
+        f = OracleFunc(mode)
+    else:
+        raise RuntimeError("unrecognized mode")
+    if 'dtype' in kwargs:
+        f.dtype = kwargs['dtype']
+    return f
+
+
+# ----------------------------------------------------------------------------------------
+# Buckets  (src/bucketing.py:6-36)
+# ----------------------------------------------------------------------------------------
+
+BUCKET_SIZES = [2 ** s for s in range(7, 31)]
+
+
+def get_next_bucket_size(s):
+    for b in BUCKET_SIZES:
+        if s <= b:
+            return b
+    raise ValueError("max bucket size exceeded")
+
+
+def fits_in_smaller_bucket(size, curr_bucket_size):
+    return get_next_bucket_size(size) < curr_bucket_size
+
+
+# ----------------------------------------------------------------------------------------
+# Ray casting  (src/queries.py:23-175, src/render.py:17-50)
+# ----------------------------------------------------------------------------------------
+
+def get_default_cast_opts():
+    """src/queries.py:23-36."""
+    return {'hit_eps': 0.001, 'max_dist': 10., 'n_max_step': 512, 'n_substeps': 1,
+            'safety_factor': 0.98, 'interval_grow_fac': 1.5, 'interval_shrink_fac': 0.5,
+            'interval_init_size': 0.1, 'refine_width_fac': 2., 'n_side_init': 16}
+
+
+def cast_rays(funcs, params_list, roots, dirs, opts):
+    """src/queries.py:39-175.  Each ray steps independently; the bucketing only changes
+    ``N_evals``, which is reproduced by replaying the bucket sizes."""
+    f32 = funcs[0].dtype
+    roots = np.asarray(roots, f32)
+    dirs = np.asarray(dirs, f32)
+    N = roots.shape[0]
+    hit_eps = opts['hit_eps']
+    out_t = np.zeros(N, f32)
+    out_hit = np.zeros(N, np.int32)
+    out_count = np.zeros(N, np.int32)
+    t = np.zeros(N, f32)
+    step = (np.ones(N, f32) * opts['interval_init_size'] * opts['max_dist']).astype(f32)
+    count = np.zeros(N, np.int32)
+    active = np.arange(N)
+    bucket = N
+    n_evals = 0
+    n_sub = opts['n_substeps']
+    while True:
+        r, d = roots[active], dirs[active]
+        tt, ss = t[active], step[active]
+        is_hit = np.zeros(active.shape[0], bool)
+        hit_id = np.zeros(active.shape[0], np.int32)
+        n_inner = np.zeros(active.shape[0], np.int32)
+        for _ in range(n_sub):                              # src/queries.py:44-92
+            can_step = ~is_hit
+            n_inner += (~is_hit).astype(np.int32)
+            for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
+                pos_start = r + tt[:, None] * d
+                half_vec = 0.5 * ss[:, None] * d
+                pos_mid = pos_start + half_vec
+                btype = func.classify_general_box(params, pos_mid, half_vec[:, None, :])
+                can_step &= (btype == SIGN_POSITIVE) | (btype == SIGN_NEGATIVE)
+                pos_eps = r + (tt + np.asarray(hit_eps, f32))[:, None] * d
+                v0 = func(params, pos_start)
+                v1 = func(params, pos_eps)
+                this_hit = np.sign(v0) != np.sign(v1)
+                hit_id = np.where(this_hit, fid, hit_id).astype(np.int32)
+                is_hit |= this_hit
+            this_step = np.where(can_step, ss, np.asarray(hit_eps, f32)).astype(f32)
+            tt = np.where(is_hit, tt, tt + this_step * np.asarray(opts['safety_factor'], f32)).astype(f32)
+            ss = np.where(can_step, ss * np.asarray(opts['interval_grow_fac'], f32),
+                          ss * np.asarray(opts['interval_shrink_fac'], f32)).astype(f32)
+            ss = np.maximum(ss, np.asarray(hit_eps, f32)).astype(f32)
+        n_evals += bucket * n_sub
+        t[active], step[active] = tt, ss
+        count[active] += n_inner
+        c = count[active]
+        term = is_hit | (tt > opts['max_dist']) | (c >= opts['n_max_step'])  # :116-120
+        done = active[term]
+        out_t[done] = tt[term]
+        out_hit[done] = hit_id[term]
+        out_count[done] = c[term]
+        active = active[~term]
+        n_valid = active.shape[0]
+        if n_valid == 0:
+            break
+        if fits_in_smaller_bucket(n_valid, bucket):
+            bucket = get_next_bucket_size(n_valid)
+    return out_t, out_hit, out_count, n_evals
+
+
+def jax_linspace(start, stop, num, dtype=np.float32):
+    """``jnp.linspace`` for floats: ``start * (1 - s) + stop * s`` with ``s = i / (num - 1)``,
+    which keeps both endpoints exact (the formula of jax.numpy's linspace).  ``start`` and
+    ``stop`` broadcast against a trailing axis of length ``num``."""
+    s = (np.arange(num, dtype=dtype) / np.asarray(num - 1, dtype)).astype(dtype)
+    return (np.asarray(start, dtype) * (1 - s) + np.asarray(stop, dtype) * s).astype(dtype)
+
+
+def normalize(x):
+    return x / np.linalg.norm(x, axis=-1, keepdims=True)
+
+
+def generate_camera_rays(eye_pos, look_dir, up_dir, res=1024, fov_deg=30., dtype=np.float32):
+    """src/render.py:26-50 (pinhole, x fastest, image coords linspace(-1, 1, res))."""
+    eye_pos = np.asarray(eye_pos, dtype)
+    look_dir = np.asarray(look_dir, dtype)
+    up_dir = np.asarray(up_dir, dtype)
+    ax = jax_linspace(np.asarray(-1., dtype), np.asarray(1., dtype), res, dtype)
+    cx, cy = np.meshgrid(ax, ax)
+    cx, cy = cx.reshape(-1), cy.reshape(-1)
+    up_dir = up_dir - np.dot(look_dir, up_dir) * look_dir
+    up_dir = normalize(up_dir)
+    left_dir = np.cross(look_dir, up_dir).astype(dtype)
+    tanf = np.asarray(np.tan(np.deg2rad(fov_deg) / 2), dtype)
+    p = look_dir[None, :] + left_dir[None, :] * (cx * tanf)[:, None] + up_dir[None, :] * (cy * tanf)[:, None]
+    dirs = normalize(p).astype(dtype)
+    roots = np.tile(eye_pos, (dirs.shape[0], 1))
+    return roots, dirs
+
+
+def look_at(eye_pos, target=None, up_dir='y', dtype=np.float32):
+    """src/render.py:229-242."""
+    eye_pos = np.asarray(eye_pos, dtype)
+    target = np.zeros(3, dtype) if target is None else np.asarray(target, dtype)
+    up = np.asarray((0., 1., 0.) if up_dir == 'y' else (0., 0., 1.), dtype)
+    look = normalize(target - eye_pos)
+    up = normalize(up - np.dot(up, look) * look)
+    left = np.cross(look, up)
+    return look.astype(dtype), up.astype(dtype), left.astype(dtype)
+
+
+# ----------------------------------------------------------------------------------------
+# Level-set kd-tree  (src/kd_tree.py:19-218)
+# ----------------------------------------------------------------------------------------
+
+def split_children(lower, upper):
+    """Children of a bisection along the first longest axis (src/kd_tree.py:38,70-77)."""
+    split_dim = np.argmax(upper - lower, axis=-1)
+    mid = 0.5 * (lower + upper)
+    mask = np.arange(3)[None, :] == split_dim[:, None]
+    a_lo, a_hi = lower, np.where(mask, mid, upper)
+    b_lo, b_hi = np.where(mask, mid, lower), upper
+    return (a_lo, a_hi), (b_lo, b_hi)
+
+
+def construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_terminate_thresh=None,
+                                            split_depth=None, with_interior_nodes=False,
+                                            with_exterior_nodes=False, offset=0.,
+                                            batch_process_size=2048):
+    """src/kd_tree.py:103-218.  Returns exactly sized arrays (no bucket padding) in the
+    reference's order: per batch of ``batch_process_size`` nodes, the A children then
+    the B children of its unknown nodes."""
+    if node_terminate_thresh is None and split_depth is None:
+        raise ValueError("must specify at least one of node_terminate_thresh or split_depth")
+    if node_terminate_thresh is None:
+        node_terminate_thresh = 9999999999
+    dt = func.dtype
+    node_lo = np.asarray(lower, dt)[None, :]
+    node_hi = np.asarray(upper, dt)[None, :]
+    n_splits = 99999999 if split_depth is None else split_depth + 1
+    interior, exterior = [], []
+    n_boxes = 0
+    for i_split in range(n_splits):
+        n_curr = node_lo.shape[0]
+        quit_next = (n_curr >= node_terminate_thresh) or (i_split + 1 == n_splits)
+        bucket = max(get_next_bucket_size(n_curr), 1) if i_split > 0 else 1
+        this_b = min(batch_process_size, bucket)
+        types = func.classify_box(params, node_lo, node_hi, offset=offset) if n_curr else np.zeros(0, np.int32)
+        n_boxes += n_curr
+        if with_interior_nodes:
+            m = types == SIGN_NEGATIVE
+            interior.append((node_lo[m], node_hi[m]))
+        if with_exterior_nodes:
+            m = types == SIGN_POSITIVE
+            exterior.append((node_lo[m], node_hi[m]))
+        unk = types == SIGN_UNKNOWN
+        if not quit_next:
+            los, his = [], []
+            for s in range(0, n_curr, this_b):
+                sl = slice(s, s + this_b)
+                m = unk[sl]
+                (alo, ahi), (blo, bhi) = split_children(node_lo[sl][m], node_hi[sl][m])
+                los += [alo, blo]
+                his += [ahi, bhi]
+            node_lo = np.concatenate(los) if los else np.zeros((0, 3), dt)
+            node_hi = np.concatenate(his) if his else np.zeros((0, 3), dt)
+        else:
+            node_lo, node_hi = node_lo[unk], node_hi[unk]
+            break
+    out = {'unknown_node_valid': np.ones(node_lo.shape[0], bool),
+           'unknown_node_lower': node_lo, 'unknown_node_upper': node_hi,
+           'n_boxes_classified': n_boxes}
+    for name, lst, flag in (('interior', interior, with_interior_nodes),
+                            ('exterior', exterior, with_exterior_nodes)):
+        if flag:
+            lo = np.concatenate([a for a, _ in lst]) if lst else np.zeros((0, 3), dt)
+            hi = np.concatenate([b for _, b in lst]) if lst else np.zeros((0, 3), dt)
+            out[f'{name}_node_valid'] = np.ones(lo.shape[0], bool)
+            out[f'{name}_node_lower'] = lo
+            out[f'{name}_node_upper'] = hi
+    return out
+
+
+# ----------------------------------------------------------------------------------------
+# Hierarchical marching cubes  (src/kd_tree.py:338-399, src/extract_cell.py:306-421)
+# ----------------------------------------------------------------------------------------
+
+def extract_triangles_from_subcells(func, params, mc_data, n_sub_depth, cell_lo, cell_hi):
+    """src/extract_cell.py:366-421 batched over leaves: returns tris (L, S*5, 3, 3) and
+    valid (L, S*5)."""
+    tri_table, edge_verts, vert_logical = mc_data
+    dt = func.dtype
+    L = cell_lo.shape[0]
+    ns = 2 ** n_sub_depth
+    npts = ns + 1
+    # jnp.linspace(lo, hi, num): lo + i * (hi - lo) / (num - 1), endpoint exact
+    coords = [jax_linspace(cell_lo[:, k:k + 1], cell_hi[:, k:k + 1], npts, dt) for k in range(3)]
+    gx = np.broadcast_to(coords[0][:, :, None, None], (L, npts, npts, npts))
+    gy = np.broadcast_to(coords[1][:, None, :, None], (L, npts, npts, npts))
+    gz = np.broadcast_to(coords[2][:, None, None, :], (L, npts, npts, npts))
+    pts = np.stack((gx, gy, gz), axis=-1).reshape(-1, 3)
+    vals = func(params, pts).reshape(L, npts, npts, npts)
+    si = np.stack(np.meshgrid(np.arange(ns), np.arange(ns), np.arange(ns), indexing='ij'), axis=-1).reshape(-1, 3)
+    delta = (cell_hi - cell_lo) / np.asarray(ns, dt)
+    sub_lo = cell_lo[:, None, :] + si[None, :, :].astype(dt) * delta[:, None, :]
+    sub_hi = sub_lo + delta[:, None, :]
+    vinds = si[:, None, :] + vert_logical[None, :, :].astype(np.int64)          # (S, 8, 3)
+    vvals = vals[:, vinds[..., 0], vinds[..., 1], vinds[..., 2]]               # (L, S, 8)
+    vpos = np.where(vert_logical[None, None, :, :], sub_hi[:, :, None, :], sub_lo[:, :, None, :])  # (L,S,8,3)
+    # extract_triangles_from_cell (src/extract_cell.py:314-364)
+    iA, iB = edge_verts[:, 0], edge_verts[:, 1]
+    vA, vB = vvals[:, :, iA], vvals[:, :, iB]
+    with np.errstate(divide='ignore', invalid='ignore'):
+        tc = -vA / (vB - vA)
+    tc = np.clip(np.nan_to_num(tc), 0, 1)
+    eloc = (1. - tc)[..., None] * vpos[:, :, iA, :] + tc[..., None] * vpos[:, :, iB, :]  # (L,S,12,3)
+    case = np.sum((vvals < 0).astype(np.int64) << np.arange(8)[None, None, :], axis=-1)  # (L,S)
+    tris_e = tri_table[case][..., :15].reshape(L, -1, 5, 3)                       # (L,S,5,3)
+    valid = tris_e[..., 0] != -1
+    ei = np.clip(tris_e, 0, None)
+    Ls, Ss = np.meshgrid(np.arange(L), np.arange(eloc.shape[1]), indexing='ij')
+    tri = eloc[Ls[:, :, None, None], Ss[:, :, None, None], ei]                    # (L,S,5,3,3)
+    return tri.reshape(L, -1, 3, 3), valid.reshape(L, -1)
+
+
+def hierarchical_marching_cubes(func, params, lower, upper, depth, mc_data, n_subcell_depth=2):
+    """src/kd_tree.py:357-399; returns (T, 3, 3) in the reference's order."""
+    tree = construct_uniform_unknown_levelset_tree(func, params, lower, upper,
+                                                   split_depth=3 * (depth - n_subcell_depth))
+    lo, hi = tree['unknown_node_lower'], tree['unknown_node_upper']
+    if lo.shape[0] == 0:
+        return np.zeros((0, 3, 3), func.dtype)
+    out = []
+    for s in range(0, lo.shape[0], 4096):
+        tri, valid = extract_triangles_from_subcells(func, params, mc_data, n_subcell_depth,
+                                                     lo[s:s + 4096], hi[s:s + 4096])
+        out.append(tri[valid])
+    return np.concatenate(out)
+
+
+# ----------------------------------------------------------------------------------------
+# Pairwise intersection  (src/kd_tree.py:402-655)
+# ----------------------------------------------------------------------------------------
+
+def _sample_offsets(d=3):
+    return np.concatenate((np.zeros((1, d)), np.eye(d), -np.eye(d)), axis=0)  # (7, d)
+
+
+def find_any_intersection(funcs, params_list, lower, upper, eps, max_rounds=200):
+    """src/kd_tree.py:402-655.  Returns (found, loc, n_nodes_processed)."""
+    fA, fB = funcs
+    pA, pB = params_list
+    dt = fA.dtype
+    lo = np.asarray(lower, dt)[None, :]
+    hi = np.asarray(upper, dt)[None, :]
+    eps_w = np.asarray(eps / np.sqrt(np.asarray(3., dt)), dt)
+    offs = _sample_offsets().astype(dt)
+    processed = 0
+    for _ in range(max_rounds):
+        n = lo.shape[0]
+        if n == 0:
+            return False, np.array((-777., -777., -777.), dt), processed
+        processed += n
+        width = np.max(hi - lo, axis=-1)
+        small = width < eps_w
+        center = 0.5 * (lo + hi)
+        pts = center[:, None, :] + eps_w * offs[None, :, :]                     # (n,7,3)
+        tA = fA.classify_box(pA, lo, hi)
+        tB = fB.classify_box(pB, lo, hi)
+        sA = fA(pA, pts.reshape(-1, 3)).reshape(n, 7)
+        sB = fB(pB, pts.reshape(-1, 3)).reshape(n, 7)
+        same = lambda s: np.all(s < 0, axis=1) | np.all(s > 0, axis=1)
+        nearA = small & ~same(sA)
+        nearB = small & ~same(sB)
+        found = np.zeros(n, bool)
+        loc = np.full((n, 3), -777., dt)
+        iA = np.argmax(sA < 0, axis=1)
+        iB = np.argmax(sB < 0, axis=1)
+        anyA = sA[np.arange(n), iA] < 0
+        anyB = sB[np.arange(n), iB] < 0
+        near_neg = small & anyA & anyB
+        found |= near_neg
+        locA = pts[np.arange(n), iA]
+        locB = pts[np.arange(n), iB]
+        loc = np.where(near_neg[:, None], 0.5 * (locA + locB), loc)
+        both = (sA < 0) & (sB < 0)
+        ib = np.argmax(both, axis=1)
+        has_both = both[np.arange(n), ib]
+        found |= has_both
+        loc = np.where(has_both[:, None], pts[np.arange(n), ib], loc)
+        cinA = (tA == SIGN_NEGATIVE) | ((tA == SIGN_UNKNOWN) & ~nearA)
+        cinB = (tB == SIGN_NEGATIVE) | ((tB == SIGN_UNKNOWN) & ~nearB)
+        if np.any(found):
+            k = int(np.argmax(found))
+            return True, loc[k], processed
+        sub = cinA & cinB
+        (alo, ahi), (blo, bhi) = split_children(lo[sub], hi[sub])
+        m = alo.shape[0]
+        lo = np.stack((alo, blo), axis=1).reshape(2 * m, 3)                     # interleave
+        hi = np.stack((ahi, bhi), axis=1).reshape(2 * m, 3)
+    raise RuntimeError("intersection search did not terminate")
+
+
+# ----------------------------------------------------------------------------------------
+# Closest point  (src/kd_tree.py:659-802)
+# ----------------------------------------------------------------------------------------
+
+def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048):
+    """src/kd_tree.py:659-802 with the same global LIFO stack and batch pops."""
+    dt = func.dtype
+    q = np.asarray(query_points, dt)
+    Q = q.shape[0]
+    B = batch_process_size
+    st_lo = np.repeat(np.asarray(lower, dt)[None, :], Q, axis=0)
+    st_hi = np.repeat(np.asarray(upper, dt)[None, :], Q, axis=0)
+    st_id = np.arange(Q)
+    top = Q
+    min_dist = np.full(Q, np.inf, dt)
+    min_loc = np.full((Q, 3), -777., dt)
+    eps_w = np.asarray(eps / np.sqrt(np.asarray(3., dt)), dt)
+    offs = _sample_offsets().astype(dt)
+    rounds = 0
+    while top > 0:
+        pop = max(top - B, 0)
+        lo, hi, ids = st_lo[pop:top], st_hi[pop:top], st_id[pop:top]
+        n = top - pop
+        ql = q[ids]
+        qmd = min_dist[ids]
+        width = np.max(hi - lo, axis=-1)
+        center = 0.5 * (lo + hi)
+        diag = np.sqrt(np.sum(np.square(hi - lo), axis=-1))
+        cdist = np.linalg.norm(ql - center, axis=-1).astype(dt)
+        max_d = cdist + diag
+        small = width < eps_w
+        pts = center[:, None, :] + (hi - lo)[:, None, :] * offs[None, :, :]
+        types = func.classify_box(params, lo, hi)
+        outside = (types == SIGN_NEGATIVE) | (types == SIGN_POSITIVE)
+        sv = func(params, pts.reshape(-1, 3)).reshape(n, 7)
+        spans = ~(np.all(sv < 0, axis=1) | np.all(sv > 0, axis=1))
+        this_d = np.where(spans, max_d, np.inf).astype(dt)
+        needs = (~outside) & (~small) & (cdist < qmd)
+        np.minimum.at(min_dist, ids, this_d)
+        newmin = this_d == min_dist[ids]
+        min_loc[ids[newmin]] = center[newmin]   # scatter-set; the last duplicate wins
+        (alo, ahi), (blo, bhi) = split_children(lo[needs], hi[needs])
+        m = alo.shape[0]
+        new_lo = np.stack((alo, blo), axis=1).reshape(2 * m, 3)
+        new_hi = np.stack((ahi, bhi), axis=1).reshape(2 * m, 3)
+        new_id = np.repeat(ids[needs], 2)
+        st_lo = np.concatenate((st_lo[:pop], new_lo))
+        st_hi = np.concatenate((st_hi[:pop], new_hi))
+        st_id = np.concatenate((st_id[:pop], new_id))
+        top = pop + 2 * m
+        rounds += 1
+    return min_dist, min_loc

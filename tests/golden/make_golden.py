@@ -1,0 +1,215 @@
+"""Generate the golden vectors in this folder by running the reference's own code.
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+The reference (nmwsharp/neural-implicit-queries) is pure JAX and JAX is not installed
+here, so its ``src/*.py`` modules are imported unchanged over the NumPy stand-in in
+``jax_standin.py``.  Inputs are seeded synthetic models (``workloads.he_mlp``) and
+seeded boxes/rays/queries; each ``.npz`` written here holds the model parameters, the
+inputs and the reference's outputs, so the tests that read them need neither the
+reference nor this script.  Only this script reads the reference tree.
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import importlib
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+import jax_standin  # noqa: E402
+
+workloads = importlib.import_module('neural-implicit-queries_gb300.workloads')
+
+
+def flat(prefix, params):
+    return {f'{prefix}/{k}': np.asarray(v) for k, v in params.items()}
+
+
+def rand_boxes(rng, n, v):
+    """Boxes for the bound cases: centers in [-1,1]^3, half extents log-uniform in
+    [1e-3, 0.5]; v=3 axis-aligned diagonal vecs, v=1 ray segments, v=2 random."""
+    center = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    if v == 3:
+        half = np.exp(rng.uniform(np.log(1e-3), np.log(0.5), (n, 3))).astype(np.float32)
+        vecs = np.zeros((n, 3, 3), np.float32)
+        vecs[:, np.arange(3), np.arange(3)] = half
+    else:
+        vecs = rng.standard_normal((n, v, 3)).astype(np.float32)
+        vecs *= (np.exp(rng.uniform(np.log(1e-3), np.log(0.3), (n, v, 1))) /
+                 np.linalg.norm(vecs, axis=-1, keepdims=True)).astype(np.float32)
+    return center, vecs.astype(np.float32)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--reference', default='/root/reference')
+    args = ap.parse_args()
+    jax_standin.install()
+    sys.path.insert(0, os.path.join(args.reference, 'src'))
+    import jax.numpy as jnp
+    import affine, mlp, implicit_mlp_utils, slope_interval, queries, kd_tree, extract_cell  # noqa
+
+    tmp = tempfile.mkdtemp()
+
+    def load_as_reference(params, name, mode, **kw):
+        path = os.path.join(tmp, name + '.npz')
+        np.savez(path, **params)
+        return implicit_mlp_utils.generate_implicit_from_file(path, mode=mode, **kw)
+
+    models = {
+        'relu16': workloads.he_mlp([3, 16, 16, 1], 'relu', seed=0),
+        'elu16': workloads.he_mlp([3, 16, 16, 1], 'elu', seed=1),
+        'relu32x3': workloads.plain_small_model(),
+    }
+    t0 = time.time()
+
+    # ---------------------------------------------------------------- point evals + bounds
+    mode_kw = {'interval': {}, 'affine_fixed': {}, 'affine_all': {},
+               'affine_truncate': {'affine_n_truncate': 8, 'affine_truncate_policy': 'absolute'},
+               'affine_append': {'affine_n_append': 4}, 'slope_interval': {}}
+    out = {}
+    rng = np.random.default_rng(1234)
+    for mname, params in models.items():
+        out.update(flat(f'model/{mname}', params))
+        pts = rng.uniform(-1.2, 1.2, (128, 3)).astype(np.float32)
+        f, p = load_as_reference(params, mname, 'affine_fixed')
+        out[f'points/{mname}/x'] = pts
+        out[f'points/{mname}/f'] = np.asarray(jax_standin._vmap(lambda x: f(p, x))(pts))
+        for v in (3, 1, 2):
+            center, vecs = rand_boxes(rng, 48, v)
+            out[f'boxes/{mname}/v{v}/center'] = center
+            out[f'boxes/{mname}/v{v}/vecs'] = vecs
+            for mode, kw in mode_kw.items():
+                f, p = load_as_reference(params, mname, mode, **kw)
+                if mode == 'slope_interval':
+                    def bounds_one(c, vv):
+                        inp = slope_interval.coordinates_in_general_box(c, vv)
+                        o = f.slope_interval_func(p, inp)
+                        sl, su = slope_interval.slope_bounds(o)
+                        return slope_interval.primal_may_contain_bounds(o, sl, su)
+                else:
+                    def bounds_one(c, vv):
+                        ctx = dataclasses.replace(f.ctx, affine_domain_terms=vv.shape[0])
+                        inp = affine.coordinates_in_general_box(ctx, c, vv)
+                        o = f.affine_func(p, inp, {'ctx': ctx})
+                        return affine.may_contain_bounds(ctx, o)
+                lo, hi = jax_standin._vmap(bounds_one)(center, vecs)
+                sign = jax_standin._vmap(lambda c, vv: f.classify_general_box(p, c, vv, offset=0.01))(center, vecs)
+                out[f'boxes/{mname}/v{v}/{mode}/lower'] = np.asarray(lo)
+                out[f'boxes/{mname}/v{v}/{mode}/upper'] = np.asarray(hi)
+                out[f'boxes/{mname}/v{v}/{mode}/sign_off0.01'] = np.asarray(sign)
+    np.savez_compressed(os.path.join(HERE, 'bounds.npz'), **out)
+    print(f'bounds done {time.time() - t0:.1f}s', flush=True)
+
+    # ---------------------------------------------------------------- cast_rays
+    out = {}
+    params = models['relu32x3']
+    out.update(flat('model/relu32x3', params))
+    out.update(flat('model/relu16', models['relu16']))
+    eye = np.array([0., 0., 3.], np.float32)
+    look, up, left = (np.array(v, np.float32) for v in ([0, 0, -1.], [0, 1., 0], [1., 0, 0]))
+    roots, dirs = (np.asarray(a) for a in _camera(eye, look, up, 20, 60.))
+    out['rays/roots'], out['rays/dirs'] = roots, dirs
+    for mode in ('affine_fixed', 'interval', 'slope_interval'):
+        f, p = load_as_reference(params, 'relu32x3', mode)
+        opts = queries.get_default_cast_opts()
+        opts['n_max_step'] = 64
+        t, hid, cnt, nev = queries.cast_rays((f,), (p,), jnp.array(roots), jnp.array(dirs), opts)
+        out[f'rays/{mode}/t'], out[f'rays/{mode}/hit_id'] = np.asarray(t), np.asarray(hid)
+        out[f'rays/{mode}/count'], out[f'rays/{mode}/n_evals'] = np.asarray(cnt), np.asarray(nev)
+        print(f'rays {mode} {time.time() - t0:.1f}s', flush=True)
+    # two functions, the second one shifted
+    f1, p1 = load_as_reference(params, 'relu32x3', 'affine_fixed')
+    f2, p2 = load_as_reference(models['relu16'], 'relu16', 'affine_fixed')
+    opts = queries.get_default_cast_opts()
+    opts['n_max_step'] = 48
+    opts['n_substeps'] = 2
+    sub = slice(0, roots.shape[0], 3)
+    t, hid, cnt, nev = queries.cast_rays((f1, f2), (p1, p2), jnp.array(roots[sub]), jnp.array(dirs[sub]), opts)
+    out['rays2/t'], out['rays2/hit_id'], out['rays2/count'] = np.asarray(t), np.asarray(hid), np.asarray(cnt)
+    out['rays2/n_evals'] = np.asarray(nev)
+    np.savez_compressed(os.path.join(HERE, 'rays.npz'), **out)
+    print(f'rays done {time.time() - t0:.1f}s', flush=True)
+
+    # ---------------------------------------------------------------- tree, hmc
+    out = {}
+    out.update(flat('model/relu32x3', params))
+    lower = jnp.array((-1., -1., -1.))
+    upper = jnp.array((1., 1., 1.))
+    for mode in ('affine_fixed', 'interval'):
+        f, p = load_as_reference(params, 'relu32x3', mode)
+        d = kd_tree.construct_uniform_unknown_levelset_tree(f, p, lower, upper, split_depth=9,
+                                                            with_interior_nodes=True,
+                                                            with_exterior_nodes=True, offset=0.)
+        for kind in ('unknown', 'interior', 'exterior'):
+            valid = np.asarray(d[f'{kind}_node_valid'])
+            out[f'tree/{mode}/{kind}/lower'] = np.asarray(d[f'{kind}_node_lower'])[valid]
+            out[f'tree/{mode}/{kind}/upper'] = np.asarray(d[f'{kind}_node_upper'])[valid]
+    f, p = load_as_reference(params, 'relu32x3', 'affine_fixed')
+    d = kd_tree.construct_uniform_unknown_levelset_tree(f, p, lower, upper, node_terminate_thresh=200,
+                                                        offset=0.05, batch_process_size=128)
+    valid = np.asarray(d['unknown_node_valid'])
+    out['tree_thresh/lower'] = np.asarray(d['unknown_node_lower'])[valid]
+    out['tree_thresh/upper'] = np.asarray(d['unknown_node_upper'])[valid]
+    print(f'tree done {time.time() - t0:.1f}s', flush=True)
+    tris = kd_tree.hierarchical_marching_cubes(f, p, lower, upper, 4, n_subcell_depth=1)
+    out['hmc/d4s1/tris'] = np.asarray(tris)
+    tris = kd_tree.hierarchical_marching_cubes(f, p, lower, upper, 3, n_subcell_depth=0)
+    out['hmc/d3s0/tris'] = np.asarray(tris)
+    np.savez_compressed(os.path.join(HERE, 'tree.npz'), **out)
+    print(f'hmc done {time.time() - t0:.1f}s', flush=True)
+
+    # ---------------------------------------------------------------- intersection, closest point
+    out = {}
+    # bounded shapes for the pairwise search: small MLPs fitted to spheres
+    A = workloads.fit_sdf_mlp([3, 16, 16, 1], workloads.sphere_sdf_fn([0., 0., 0.], 0.35),
+                              steps=400, lr=1e-2, seed=3, n_points=4096)
+    B = workloads.prepend_spatial_transformation(
+        workloads.fit_sdf_mlp([3, 16, 16, 1], workloads.sphere_sdf_fn([0., 0., 0.], 0.3),
+                              steps=400, lr=1e-2, seed=4, n_points=4096))
+    out.update(flat('model/A', A))
+    rot = workloads.random_rotation(np.random.default_rng(5))
+    # the shape moves by (R, t): points are mapped by x @ inv(R) + inv(R) @ (-t)
+    cases = {'near': (rot, rot @ np.array([0.55, 0.1, 0.0], np.float32)),
+             'far': (rot, rot @ np.array([0.8, 0.35, 0.0], np.float32))}
+    for name, (R, tr) in cases.items():
+        Bp = dict(B)
+        Bp['0000.spatial_transformation.R'] = R
+        Bp['0000.spatial_transformation.t'] = tr.astype(np.float32)
+        out.update(flat(f'model/B_{name}', Bp))
+        for mode in ('affine_all', 'affine_fixed'):
+            fa, pa = load_as_reference(A, 'A', mode)
+            fb, pb = load_as_reference(Bp, 'B' + name, mode)
+            found, ia, ib, loc = kd_tree.find_any_intersection((fa, fb), (pa, pb), lower, upper, 0.02)
+            out[f'isect/{name}/{mode}/found'] = np.asarray(bool(found))
+            out[f'isect/{name}/{mode}/loc'] = np.asarray(loc)
+            print(f'isect {name} {mode} found={bool(found)} {time.time() - t0:.1f}s', flush=True)
+    f, p = load_as_reference(A, 'A', 'affine_fixed')
+    q = np.random.default_rng(77).uniform(-1.2, 1.2, (20, 3)).astype(np.float32)
+    out['cp/q'] = q
+    for B_ in (8, 2048):
+        dist, loc = kd_tree.closest_point(f, p, lower, upper, jnp.array(q), eps=0.05, batch_process_size=B_)
+        out[f'cp/B{B_}/dist'] = np.asarray(dist)
+        out[f'cp/B{B_}/loc'] = np.asarray(loc)
+        print(f'cp B{B_} {time.time() - t0:.1f}s', flush=True)
+    np.savez_compressed(os.path.join(HERE, 'queries.npz'), **out)
+    print(f'all done {time.time() - t0:.1f}s')
+
+
+def _camera(eye, look, up, res, fov):
+    import render  # the reference's module (imported over the stand-in)
+    return render.generate_camera_rays(eye, look, up, res=res, fov_deg=fov)
+
+
+if __name__ == '__main__':
+    main()

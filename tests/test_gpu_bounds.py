@@ -1,0 +1,131 @@
+"""CUDA point evaluation and box bounds against the oracle (oracle/ref_np.py).
+
+Tolerances: point values within 1e-5 relative; reference-arithmetic bounds
+(conservative=False) within 3e-5 of the bound scale max(|lo|,|hi|)+1e-3; conservative
+bounds contain every FP64 sample of the network inside the box (zero violations) and
+stay within 1e-4 relative width of the FP64 oracle's bounds."""
+import numpy as np
+import pytest
+
+from conftest import golden, model_from
+
+pytestmark = pytest.mark.gpu
+
+MODES = {'interval': {}, 'affine_fixed': {}, 'affine_all': {},
+         'affine_truncate': {'affine_n_truncate': 8}, 'affine_append': {'affine_n_append': 4},
+         'slope_interval': {}}
+
+
+def models(niq):
+    wl = niq.workloads
+    out = {}
+    for w, act, seed in [(16, 'relu', 0), (32, 'tanh', 1), (64, 'relu', 2), (100, 'elu', 3), (128, 'tanh', 4),
+                         (256, 'relu', 5)]:
+        depth = 2 if w >= 128 else 3
+        out[f'{act}{w}'] = wl.he_mlp([3] + [w] * depth + [1], act, seed=seed, grid=16)
+    return out
+
+
+def boxes(rng, n, v):
+    center = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    if v == 3:
+        half = np.exp(rng.uniform(np.log(1e-3), np.log(0.5), (n, 3))).astype(np.float32)
+        vecs = (half[:, :, None] * np.eye(3, dtype=np.float32)).astype(np.float32)
+    else:
+        vecs = rng.standard_normal((n, v, 3)).astype(np.float32)
+        vecs *= (np.exp(rng.uniform(np.log(1e-3), np.log(0.3), (n, v, 1))) /
+                 np.linalg.norm(vecs, axis=-1, keepdims=True)).astype(np.float32)
+    return center, vecs
+
+
+def gpu_func(niq, params, mode, conservative):
+    f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=conservative, **MODES[mode])
+    return f
+
+
+def test_eval_points(niq, R, gpu_ready):
+    rng = np.random.default_rng(0)
+    for name, params in models(niq).items():
+        x = rng.uniform(-1.5, 1.5, (3001, 3)).astype(np.float32)
+        f = gpu_func(niq, params, 'affine_fixed', True)
+        got = f(params, x)
+        ref = R.eval_points(params, x)
+        scale = np.abs(ref).max() + 1e-3
+        assert np.max(np.abs(got - ref)) <= 1e-5 * scale, name
+
+
+def test_eval_points_golden(niq, gpu_ready):
+    g = golden('bounds.npz')
+    for m in ['relu16', 'elu16', 'relu32x3']:
+        params = model_from(g, f'model/{m}')
+        f = gpu_func(niq, params, 'affine_fixed', True)
+        got = f(params, g[f'points/{m}/x'])
+        np.testing.assert_allclose(got, g[f'points/{m}/f'], rtol=2e-5, atol=2e-6)
+
+
+@pytest.mark.parametrize('mode', list(MODES))
+def test_bounds_match_oracle(niq, R, gpu_ready, mode):
+    rng = np.random.default_rng(1)
+    for name, params in models(niq).items():
+        for v in (3, 1, 2):
+            c, vv = boxes(rng, 97, v)
+            f = gpu_func(niq, params, mode, conservative=False)
+            sign, lo, hi = f.bounds_general_box(params, c, vv, offset=0.)
+            o = R.generate_implicit(params, mode, **MODES[mode])
+            rlo, rhi = o.bounds_general(params, c, vv)
+            scale = np.maximum(np.abs(rlo), np.abs(rhi)) + 1e-3
+            err = max(np.max(np.abs(lo - rlo) / scale), np.max(np.abs(hi - rhi) / scale))
+            assert err <= 3e-5, (name, v, err)
+            rs = R.sign_from_bounds(rlo, rhi)
+            near = (np.abs(rlo) < 1e-4 * scale) | (np.abs(rhi) < 1e-4 * scale)
+            assert np.all((sign == rs) | near), (name, v)
+
+
+@pytest.mark.parametrize('mode', list(MODES))
+def test_bounds_golden(niq, gpu_ready, mode):
+    g = golden('bounds.npz')
+    for m in ['relu16', 'elu16', 'relu32x3']:
+        params = model_from(g, f'model/{m}')
+        for v in (3, 1, 2):
+            c, vv = g[f'boxes/{m}/v{v}/center'], g[f'boxes/{m}/v{v}/vecs']
+            f = gpu_func(niq, params, mode, conservative=False)
+            sign, lo, hi = f.bounds_general_box(params, c, vv, offset=0.01)
+            glo, ghi = g[f'boxes/{m}/v{v}/{mode}/lower'], g[f'boxes/{m}/v{v}/{mode}/upper']
+            scale = np.maximum(np.abs(glo), np.abs(ghi)) + 1e-3
+            assert np.max(np.abs(lo - glo) / scale) <= 3e-5 and np.max(np.abs(hi - ghi) / scale) <= 3e-5, (m, v)
+            gs = g[f'boxes/{m}/v{v}/{mode}/sign_off0.01']
+            near = (np.abs(glo - 0.01) < 1e-4 * scale) | (np.abs(ghi + 0.01) < 1e-4 * scale)
+            assert np.all((sign == gs) | near)
+
+
+@pytest.mark.parametrize('mode', list(MODES))
+def test_conservative_containment(niq, R, gpu_ready, mode):
+    """Zero FP64 samples outside the conservative bound; width within 1e-4 of FP64."""
+    rng = np.random.default_rng(2)
+    for name, params in models(niq).items():
+        for v in (3, 1):
+            c, vv = boxes(rng, 61, v)
+            f = gpu_func(niq, params, mode, conservative=True)
+            sign, lo, hi = f.bounds_general_box(params, c, vv)
+            # samples: all 2^v corners plus random interior points, evaluated in FP64
+            corners = np.array(np.meshgrid(*[[-1., 1.]] * v, indexing='ij')).reshape(v, -1).T
+            eps = np.concatenate([corners, rng.uniform(-1, 1, (256, v))])
+            pts = c[None].astype(np.float64) + np.einsum('sv,nvd->snd', eps, vv.astype(np.float64))
+            vals = R.eval_points(params, pts.reshape(-1, 3), np.float64).reshape(eps.shape[0], -1)
+            assert np.all(vals >= lo[None]) and np.all(vals <= hi[None]), name
+            o = R.generate_implicit(params, mode, dtype=np.float64, **MODES[mode])
+            rlo, rhi = o.bounds_general(params, c.astype(np.float64), vv.astype(np.float64))
+            w64 = rhi - rlo
+            assert np.all((hi - lo) <= w64 * (1 + 1e-4) + 1e-5 * (np.abs(rlo) + np.abs(rhi)) + 1e-6), name
+
+
+def test_errors(niq, gpu_ready):
+    wl = niq.workloads
+    params = wl.he_mlp([3, 16, 1], 'relu', seed=0, grid=8)
+    f = gpu_func(niq, params, 'affine_fixed', True)
+    with pytest.raises(ValueError):
+        f.bounds_general_box(params, np.zeros((2, 3), np.float32), np.zeros((2, 4, 3), np.float32))
+    bad = dict(params)
+    bad['0001.sin._'] = np.zeros(0, np.float32)
+    with pytest.raises(ValueError):
+        f(bad, np.zeros((1, 3), np.float32))
