@@ -168,15 +168,22 @@ int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32
  * Extracts triangles (n_tris_out[0] of them, <= tri_capacity) from the n_leaves
  * boxes (lower/upper (n_leaves,3), e.g. niq_tree_result kind 0) on a
  * (2^n_subcell_depth)^3 subgrid each.  tris_out is (tri_capacity, 3, 3). */
+size_t niq_hmc_workspace_size(void);
 int niq_hmc_extract(const niq_model* model, int64_t n_leaves, const float* leaf_lower,
                     const float* leaf_upper, int32_t n_subcell_depth,
-                    float* tris_out, int64_t tri_capacity, int64_t* n_tris_out, void* stream);
+                    float* tris_out, int64_t tri_capacity, int64_t* n_tris_out,
+                    void* workspace, size_t workspace_bytes, void* stream);
+/* The 256x16 triangle table used by niq_hmc_extract (host int32 out[256*16]; -1 pads).
+ * Same polygons and orientation as src/extract_cell.py:12-268 for every case; pure
+ * host code, no device needed. */
+int niq_mc_table(int32_t* out);
 
 /* ---- pairwise intersection: find_any_intersection (src/kd_tree.py:402-655) ---------- *
  * found_out (device int32[1]) = 1 when an intersection is found, loc_out (device
  * float[3]) its witness, (-777,-777,-777) otherwise.  Persistent kernel over all depths;
  * counts_out (device int64[2]) = {nodes processed, depth reached}. */
-size_t niq_intersect_workspace_size(int64_t node_capacity);
+size_t niq_intersect_workspace_size(const niq_model* model_a, const niq_model* model_b,
+                                    const niq_bound_opts* opts, int64_t node_capacity);
 int niq_find_any_intersection(const niq_model* model_a, const niq_model* model_b,
                               const niq_bound_opts* opts, const float* lower, const float* upper,
                               float eps, int64_t node_capacity, int32_t* found_out, float* loc_out,

@@ -1,0 +1,400 @@
+// k_rays.cu -- queries.cast_rays (src/queries.py:39-175) on the GPU.
+//
+// Per ray and step (src/queries.py:44-92), for each function of funcs_tuple:
+//   pos_start = root + t dir; half = 0.5 step dir; pos_mid = pos_start + half
+//   box_type  = classify_general_box(pos_mid, [half])       (one noise row)
+//   val_start = f(pos_start); val_eps = f(root + (t + hit_eps) dir)
+//   hit when sign(val_start) != sign(val_eps)
+// then t advances by step*safety when every function classified the segment, else by
+// hit_eps*safety; step grows or shrinks and is clipped at hit_eps.  A ray terminates on
+// a hit, t > max_dist or count >= n_max_step, checked after n_substeps steps
+// (src/queries.py:113-120).
+//
+// The bound and the two point values of one step are three row groups of a single
+// tile-engine item, so one fused forward pass serves all three.
+//
+// k_rays<PERSISTENT=true>: CTA slots refill from a global ray counter until every ray
+// has terminated (one launch).  k_rays<PERSISTENT=false>: one reference iteration over a
+// list of live rays, appending survivors to the next list (the plain form).
+#include "niq_host.cuh"
+
+namespace niq {
+
+constexpr int kMaxFuncs = 8;
+
+struct ModelSet {
+    NiqModelRef m[kMaxFuncs];
+    int woff[kMaxFuncs];   // float offset of each model's weights in the resident buffer
+    int n;
+};
+
+struct CastDev {
+    float hit_eps, max_dist, safety, grow, shrink, init_step;
+    int n_max_step, n_substeps;
+};
+
+struct RayWs {                      // device workspace header
+    unsigned long long next_ray;    // persistent: next unclaimed ray
+    unsigned long long n_live_next; // plain: survivors appended this iteration
+    int err;
+    int pad;
+};
+
+template <int TPI, bool C, bool SLOPE, bool PERSISTENT>
+__global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, long long n, const float* __restrict__ roots,
+                                               const float* __restrict__ dirs, CastDev o, float* __restrict__ t_out,
+                                               int* __restrict__ hit_out, int* __restrict__ count_out,
+                                               unsigned long long* __restrict__ n_evals, RayWs* ws,
+                                               // plain-form state (full-size arrays indexed by ray id)
+                                               float* __restrict__ st_t, float* __restrict__ st_step,
+                                               int* __restrict__ st_count, const int* __restrict__ live_in,
+                                               long long n_live, int* __restrict__ live_out,
+                                               int fixed_floats, int sw_cap, int resident) {
+    using Cfg = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT>, TileCfg<5, 1, TPI, kNT>>::type;
+    constexpr int ITEMS = Cfg::ITEMS, R = Cfg::R, LD = Cfg::LD;
+    extern __shared__ float4 smem4[];
+    float* smem = reinterpret_cast<float*>(smem4);
+    float* st = smem;
+    float* ob = st + Cfg::STATE_FLOATS;
+    float* sW = smem + fixed_floats;
+    __shared__ NiqSpecHeader H;
+    __shared__ long long s_id[ITEMS];
+    __shared__ float s_t[ITEMS], s_step[ITEMS], s_root[ITEMS][3], s_dir[ITEMS][3];
+    __shared__ int s_count[ITEMS], s_alive[ITEMS], s_hit[ITEMS], s_hitid[ITEMS], s_can[ITEMS], s_inner[ITEMS];
+    __shared__ int s_act[ITEMS];   // evaluating in this substep: alive and not hit before it
+    __shared__ unsigned long long s_evals[kMaxFuncs];
+
+    const int item = threadIdx.x / TPI, g = threadIdx.x % TPI;
+    if (threadIdx.x < kMaxFuncs) s_evals[threadIdx.x] = 0ull;
+    if (resident)
+        for (int f = 0; f < S.n; ++f) {
+            load_header(H, S.m[f].hdr);
+            __syncthreads();
+            stage_floats(sW + S.woff[f], S.m[f].w, H.n_weight_floats);
+            __syncthreads();
+        }
+    if (S.n == 1) load_header(H, S.m[0].hdr);
+    const RowPlan plan{SLOPE ? ROWS_SLOPE : ROWS_AFFINE, mode_interval ? 0 : 1, 2};
+    // rows of the two points: affine v+1, v+2; slope 2, 3
+    const int rp0 = SLOPE ? 2 : plan.v + 1;
+    const int rerr = SLOPE ? 4 : R - 1;
+
+    // ---- slot (re)fill by the owner thread of each item
+    auto claim = [&](int it) {
+        long long id = -1;
+        if (PERSISTENT) {
+            const unsigned long long k = atomicAdd(&ws->next_ray, 1ull);
+            if ((long long)k < n) id = (long long)k;
+        }
+        s_id[it] = id;
+        s_alive[it] = id >= 0;
+        if (id >= 0) {
+            s_t[it] = 0.f;
+            s_step[it] = o.init_step;
+            s_count[it] = 0;
+            for (int k = 0; k < 3; ++k) { s_root[it][k] = roots[3 * id + k]; s_dir[it][k] = dirs[3 * id + k]; }
+        }
+    };
+    long long tile_base = (long long)blockIdx.x * ITEMS;
+    if (PERSISTENT) {
+        if (g == 0) claim(item);
+    }
+    __syncthreads();
+
+    while (true) {
+        if (!PERSISTENT) {
+            if (tile_base >= n_live) break;
+            if (g == 0) {
+                const long long li = tile_base + item;
+                long long id = li < n_live ? (long long)live_in[li] : -1;
+                s_id[item] = id;
+                s_alive[item] = id >= 0;
+                if (id >= 0) {
+                    s_t[item] = st_t[id];
+                    s_step[item] = st_step[id];
+                    s_count[item] = st_count[id];
+                    for (int k = 0; k < 3; ++k) { s_root[item][k] = roots[3 * id + k]; s_dir[item][k] = dirs[3 * id + k]; }
+                }
+            }
+            __syncthreads();
+        } else {
+            if (!__syncthreads_or(s_alive[item] && g == 0)) break;
+        }
+        if (g == 0) { s_hit[item] = 0; s_hitid[item] = 0; s_inner[item] = 0; }
+        for (int sub = 0; sub < o.n_substeps; ++sub) {
+            if (g == 0) {
+                s_can[item] = !s_hit[item];
+                s_act[item] = s_alive[item] && !s_hit[item];
+                s_inner[item] += s_act[item] ? 1 : 0;
+            }
+            __syncthreads();
+            for (int f = 0; f < S.n; ++f) {
+                if (S.n > 1) load_header(H, S.m[f].hdr);
+                // build rows: thread g < 4 owns input column g
+                const bool active = s_act[item];
+                float* xs = st + item * R * LD;
+                if (g < 4) {
+                    const int k = g;
+                    for (int r = 0; r < R; ++r) xs[r * LD + k] = 0.f;
+                    if (active && k < 3) {
+                        const float t = s_t[item], sz = s_step[item];
+                        const float rt = s_root[item][k], d = s_dir[item][k];
+                        const float ps = __fadd_rn(rt, __fmul_rn(t, d));
+                        const float hv = __fmul_rn(__fmul_rn(0.5f, sz), d);
+                        const float pm = __fadd_rn(ps, hv);
+                        const float pe = __fadd_rn(rt, __fmul_rn(__fadd_rn(t, o.hit_eps), d));
+                        xs[k] = pm;
+                        xs[rp0 * LD + k] = ps;
+                        xs[(rp0 + 1) * LD + k] = pe;
+                        // gamma of this function's first layer (read from global: H may be in flux)
+                        const float gam0 = C ? __ldg(&S.m[f].hdr->layers[0].gamma) : 0.f;
+                        if (SLOPE) {
+                            xs[LD + k] = hv;
+                            xs[5 * LD + k] = C ? __fmul_ru(gam0, fabsf(hv)) : 0.f;
+                            xs[4 * LD + k] = C ? __fmul_ru(gam0, fabsf(pm)) : 0.f;
+                        } else if (mode_interval) {
+                            xs[rerr * LD + k] = C ? __fmaf_ru(gam0, fabsf(pm), fabsf(hv)) : fabsf(hv);
+                        } else {
+                            xs[LD + k] = hv;
+                            xs[rerr * LD + k] = C ? __fmul_ru(gam0, __fadd_ru(fabsf(pm), fabsf(hv))) : 0.f;
+                        }
+                    }
+                }
+                __syncthreads();
+                const int woff = resident ? S.woff[f] : 0;
+                tile_forward<Cfg, C>(H, S.m[f].w, sW + woff, sw_cap, resident, plan, st, ob);
+                if (g == 0 && active) {
+                    const float* out = ob + item * R;
+                    float lo, hi;
+                    if (SLOPE) slope_out_bounds<C>(out, plan.v, lo, hi);
+                    else affine_out_bounds<Cfg::R, C>(out, plan.v, lo, hi);
+                    const int bt = sign_of_bounds(lo, hi, 0.f);
+                    if (bt == NIQ_SIGN_UNKNOWN) s_can[item] = 0;
+                    const float v0 = out[rp0], v1 = out[rp0 + 1];
+                    const int sg0 = (v0 > 0.f) - (v0 < 0.f), sg1 = (v1 > 0.f) - (v1 < 0.f);
+                    const bool this_hit = (v0 != v0) || (v1 != v1) || sg0 != sg1;  // NaN != NaN
+                    if (this_hit) { s_hitid[item] = f + 1; s_hit[item] = 1; }
+                    atomicAdd(&s_evals[f], 1ull);
+                }
+                __syncthreads();
+            }
+            if (g == 0 && s_alive[item]) {
+                // src/queries.py:79-90
+                const bool can = s_can[item];
+                const float sz = s_step[item];
+                const float this_step = can ? sz : o.hit_eps;
+                if (!s_hit[item]) s_t[item] = __fadd_rn(s_t[item], __fmul_rn(this_step, o.safety));
+                float ns = can ? __fmul_rn(sz, o.grow) : __fmul_rn(sz, o.shrink);
+                s_step[item] = fmaxf(ns, o.hit_eps);
+            }
+            __syncthreads();
+        }
+        // ---- termination (src/queries.py:113-126) and slot refill
+        if (g == 0 && s_alive[item]) {
+            const long long id = s_id[item];
+            const int cnt = s_count[item] + s_inner[item];
+            s_count[item] = cnt;
+            const float t = s_t[item];
+            const bool term = s_hit[item] || (t > o.max_dist) || (cnt >= o.n_max_step);
+            if (term) {
+                t_out[id] = t;
+                hit_out[id] = s_hitid[item];
+                count_out[id] = cnt;
+                if (PERSISTENT) claim(item);
+                else s_alive[item] = 0;
+            } else if (!PERSISTENT) {
+                st_t[id] = t;
+                st_step[id] = s_step[item];
+                st_count[id] = cnt;
+            }
+        }
+        if (!PERSISTENT) {
+            // append survivors to the next live list (warp-aggregated)
+            const bool keep = (g == 0) && s_alive[item];
+            const long long pos = niq_warp_append(&ws->n_live_next, keep);
+            if (keep) live_out[pos] = (int)s_id[item];
+            __syncthreads();
+            tile_base += (long long)gridDim.x * ITEMS;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x < S.n && s_evals[threadIdx.x]) atomicAdd(&n_evals[threadIdx.x], s_evals[threadIdx.x]);
+}
+
+static int make_set(const niq_model* const* models, int nfunc, ModelSet& S, int& maxw, int& wfloats, int& maxlayer) {
+    NIQ_REQUIRE(models && nfunc >= 1 && nfunc <= kMaxFuncs, NIQ_ERR_INVALID_ARG, "nfunc must be in [1, %d]", kMaxFuncs);
+    S.n = nfunc;
+    maxw = 0; wfloats = 0; maxlayer = 0;
+    for (int f = 0; f < nfunc; ++f) {
+        NIQ_REQUIRE(models[f], NIQ_ERR_INVALID_ARG, "null model %d", f);
+        S.m[f] = models[f]->ref();
+        S.woff[f] = wfloats;
+        wfloats += models[f]->hdr.n_weight_floats;
+        maxw = maxw > models[f]->hdr.max_width ? maxw : models[f]->hdr.max_width;
+        const int ml = max_layer_floats(models[f]->hdr);
+        maxlayer = maxlayer > ml ? maxlayer : ml;
+    }
+    return NIQ_OK;
+}
+
+__global__ void k_ray_init(float* step, int* live, long long n, float init_step) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        step[i] = init_step;
+        live[i] = (int)i;
+    }
+}
+
+static void fill_ray_init(float* step, int* live, long long n, float init_step, cudaStream_t s) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_ray_init<<<(int)blocks, 256, 0, s>>>(step, live, n, init_step);
+}
+
+static CastDev to_dev(const niq_cast_opts& c) {
+    CastDev d;
+    d.hit_eps = c.hit_eps;
+    d.max_dist = c.max_dist;
+    d.safety = c.safety_factor;
+    d.grow = c.interval_grow_fac;
+    d.shrink = c.interval_shrink_fac;
+    // src/queries.py:148: ones(N) * interval_init_size * max_dist, in float32
+    volatile float a = 1.0f * c.interval_init_size;
+    d.init_step = a * c.max_dist;
+    d.n_max_step = c.n_max_step;
+    d.n_substeps = c.n_substeps;
+    return d;
+}
+
+}  // namespace niq
+
+using namespace niq;
+
+namespace {
+
+struct RayLayout {
+    size_t hdr = 0, t = 0, step = 0, count = 0, live0 = 0, live1 = 0, total = 0;
+};
+
+RayLayout ray_layout(long long n) {
+    RayLayout L;
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    L.hdr = 0;
+    L.t = al(sizeof(RayWs));
+    L.step = L.t + al(4 * n);
+    L.count = L.step + al(4 * n);
+    L.live0 = L.count + al(4 * n);
+    L.live1 = L.live0 + al(4 * n);
+    L.total = L.live1 + al(4 * n) + 256;
+    return L;
+}
+
+template <bool PERSISTENT>
+int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts* opts, long long n, const float* roots,
+                const float* dirs, const niq_cast_opts* cast, float* t_out, int* hit_out, int* count_out,
+                unsigned long long* n_evals, void* workspace, size_t ws_bytes, cudaStream_t s) {
+    NIQ_REQUIRE(opts && cast, NIQ_ERR_INVALID_ARG, "null options");
+    NIQ_REQUIRE(n >= 0 && n < (1ll << 31), NIQ_ERR_INVALID_ARG, "ray count %lld out of range", n);
+    NIQ_REQUIRE(cast->n_substeps >= 1 && cast->hit_eps > 0.f, NIQ_ERR_INVALID_ARG, "n_substeps >= 1 and hit_eps > 0 required");
+    const int mode = opts->mode;
+    NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
+                NIQ_ERR_UNSUPPORTED, "cast_rays supports the interval, affine_fixed and slope_interval modes (mode %d)", mode);
+    ModelSet S;
+    int maxw, wfloats, maxlayer;
+    int rc = make_set(models, nfunc, S, maxw, wfloats, maxlayer);
+    if (rc) return rc;
+    const RayLayout RL = ray_layout(n);
+    NIQ_REQUIRE(workspace && ws_bytes >= RL.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", RL.total);
+    NIQ_REQUIRE(n == 0 || (roots && dirs && t_out && hit_out && count_out && n_evals), NIQ_ERR_INVALID_ARG, "null array");
+    NIQ_CUDA(cudaMemsetAsync(n_evals, 0, sizeof(unsigned long long) * nfunc, s));
+    if (n == 0) return NIQ_OK;
+    char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    RayWs* ws = reinterpret_cast<RayWs*>(base + RL.hdr);
+    float* st_t = reinterpret_cast<float*>(base + RL.t);
+    float* st_step = reinterpret_cast<float*>(base + RL.step);
+    int* st_count = reinterpret_cast<int*>(base + RL.count);
+    int* live[2] = {reinterpret_cast<int*>(base + RL.live0), reinterpret_cast<int*>(base + RL.live1)};
+    NIQ_CUDA(cudaMemsetAsync(ws, 0, sizeof(RayWs), s));
+    const CastDev cd = to_dev(*cast);
+    const bool cons = opts->conservative != 0;
+    const bool slope = mode == NIQ_MODE_SLOPE_INTERVAL;
+    const int interval = mode == NIQ_MODE_INTERVAL;
+    const int tpi = tpi_for_width(maxw);
+    rc = NIQ_OK;
+    auto run = [&](auto kern, int R, int TPIv) -> int {
+        const int items = kNT / TPIv;
+        const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
+        SmemPlan p = plan_smem(state, wfloats, maxlayer);
+        NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * maxw, NIQ_ERR_UNSUPPORTED, "shared memory too small for width %d", maxw);
+        int r2 = prepare_kernel(kern, p.bytes);
+        if (r2) return r2;
+        if (PERSISTENT) {
+            int grid = 0;
+            r2 = persistent_grid(kern, kNT, p.bytes, (n + items - 1) / items, &grid);
+            if (r2) return r2;
+            kern<<<grid, kNT, p.bytes, s>>>(S, interval, n, roots, dirs, cd, t_out, hit_out, count_out, n_evals, ws,
+                                            nullptr, nullptr, nullptr, nullptr, 0, nullptr, p.fixed_floats, p.sw_cap,
+                                            p.resident);
+            NIQ_CUDA(cudaGetLastError());
+            return NIQ_OK;
+        }
+        // plain: host loop over iterations with a device->host count read each time
+        long long n_live = n;
+        NIQ_CUDA(cudaMemsetAsync(st_t, 0, 4 * n, s));
+        NIQ_CUDA(cudaMemsetAsync(st_count, 0, 4 * n, s));
+        fill_ray_init(st_step, live[0], n, cd.init_step, s);
+        int cur = 0;
+        int grid_max = 0;
+        r2 = persistent_grid(kern, kNT, p.bytes, (n + items - 1) / items, &grid_max);
+        if (r2) return r2;
+        while (n_live > 0) {
+            NIQ_CUDA(cudaMemsetAsync(&ws->n_live_next, 0, sizeof(unsigned long long), s));
+            long long tiles = (n_live + items - 1) / items;
+            const int grid = (int)(tiles < grid_max ? tiles : grid_max);
+            kern<<<grid, kNT, p.bytes, s>>>(S, interval, n, roots, dirs, cd, t_out, hit_out, count_out, n_evals, ws,
+                                            st_t, st_step, st_count, live[cur], n_live, live[1 - cur], p.fixed_floats,
+                                            p.sw_cap, p.resident);
+            NIQ_CUDA(cudaGetLastError());
+            unsigned long long next = 0;
+            NIQ_CUDA(cudaMemcpyAsync(&next, &ws->n_live_next, sizeof(next), cudaMemcpyDeviceToHost, s));
+            NIQ_CUDA(cudaStreamSynchronize(s));
+            n_live = (long long)next;
+            cur = 1 - cur;
+        }
+        return NIQ_OK;
+    };
+#define NIQ_RAYS(CC, SL)                                                           \
+    NIQ_DISPATCH_TPI(tpi, { rc = run(k_rays<TPI, CC, SL, PERSISTENT>, SL ? 8 : 5, TPI); })
+    if (slope) { if (cons) { NIQ_RAYS(true, true); } else { NIQ_RAYS(false, true); } }
+    else { if (cons) { NIQ_RAYS(true, false); } else { NIQ_RAYS(false, false); } }
+#undef NIQ_RAYS
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t niq_cast_rays_workspace_size(int32_t nfunc, int64_t n) {
+    (void)nfunc;
+    return ray_layout(n).total;
+}
+
+int niq_cast_rays(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts, int64_t n,
+                  const float* roots, const float* dirs, const niq_cast_opts* cast, float* t_out, int32_t* hit_id_out,
+                  int32_t* count_out, int64_t* n_evals_out, void* workspace, size_t workspace_bytes, void* stream) {
+    return launch_rays<true>(models, nfunc, opts, n, roots, dirs, cast, t_out, hit_id_out, count_out,
+                             reinterpret_cast<unsigned long long*>(n_evals_out), workspace, workspace_bytes,
+                             as_stream(stream));
+}
+
+int niq_cast_rays_plain(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts, int64_t n,
+                        const float* roots, const float* dirs, const niq_cast_opts* cast, float* t_out,
+                        int32_t* hit_id_out, int32_t* count_out, int64_t* n_evals_out, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+    return launch_rays<false>(models, nfunc, opts, n, roots, dirs, cast, t_out, hit_id_out, count_out,
+                              reinterpret_cast<unsigned long long*>(n_evals_out), workspace, workspace_bytes,
+                              as_stream(stream));
+}
+
+}  // extern "C"

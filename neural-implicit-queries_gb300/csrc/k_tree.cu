@@ -1,0 +1,341 @@
+// k_tree.cu -- construct_uniform_unknown_levelset_tree (src/kd_tree.py:19-218).
+//
+// Breadth-first: level L classifies every node of the level (classify_box, v = 3,
+// src/implicit_function.py:28-37); NEGATIVE nodes go to the interior list and POSITIVE
+// ones to the exterior list when requested; UNKNOWN nodes split at the midpoint of
+// their first longest axis into children A = [lo, hi with hi[d] = mid] and
+// B = [lo with lo[d] = mid, hi] (src/kd_tree.py:38,70-77) -- or, on the last round, are
+// the result.  A round is the last when it starts with >= node_terminate_thresh nodes
+// or is round split_depth (src/kd_tree.py:136-152).
+//
+// k_tree<COOP=true>: one cooperative launch runs every level; CTAs claim chunks of the
+// level's node array with an atomic counter, and a bounded grid barrier separates
+// levels.  k_tree<COOP=false>: one level per launch, the host reads the next level's
+// size after each (the plain form, as the reference's per-level host loop).
+// Node order inside a level is whatever the atomics produce; results are node sets.
+#include "niq_host.cuh"
+
+namespace niq {
+
+constexpr int kTreeMaxLevels = 64;
+
+struct TreeWs {
+    unsigned long long level_count[kTreeMaxLevels + 1];  // nodes of level L (append counter)
+    unsigned long long grab[kTreeMaxLevels + 1];         // claim counter of level L
+    unsigned long long n_unknown, n_interior, n_exterior, n_boxes;
+    unsigned int barrier;
+    int err;
+    int last_level;
+    int pad;
+};
+
+struct TreeBufs {
+    float* lvl_lo[2];
+    float* lvl_hi[2];
+    float* res_lo[3];   // unknown, interior, exterior
+    float* res_hi[3];
+    long long cap;
+};
+
+struct TreeParams {
+    int n_rounds;               // split_depth + 1, or kTreeMaxLevels
+    long long thresh;           // node_terminate_thresh (huge when unset)
+    float offset;
+    int with_interior, with_exterior;
+    int mode_interval;
+};
+
+__device__ __forceinline__ void put_node(float* lo, float* hi, long long i, const float* a, const float* b) {
+    lo[3 * i] = a[0]; lo[3 * i + 1] = a[1]; lo[3 * i + 2] = a[2];
+    hi[3 * i] = b[0]; hi[3 * i + 1] = b[1]; hi[3 * i + 2] = b[2];
+}
+
+template <int TPI, bool C, bool SLOPE, bool COOP>
+__global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeWs* ws, TreeBufs B, int level0,
+                                              int fixed_floats, int sw_cap, int resident) {
+    using Cfg = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT>, TileCfg<5, 1, TPI, kNT>>::type;
+    constexpr int ITEMS = Cfg::ITEMS, R = Cfg::R, LD = Cfg::LD;
+    extern __shared__ float4 smem4[];
+    float* smem = reinterpret_cast<float*>(smem4);
+    float* st = smem;
+    float* ob = st + Cfg::STATE_FLOATS;
+    float* sW = smem + fixed_floats;
+    __shared__ NiqSpecHeader H;
+    __shared__ float s_lo[ITEMS][3], s_hi[ITEMS][3];
+    __shared__ long long s_base;
+    __shared__ unsigned long long s_boxes;
+    load_header(H, M.hdr);
+    __syncthreads();
+    if (resident) stage_floats(sW, M.w, H.n_weight_floats);
+    const RowPlan plan{SLOPE ? ROWS_SLOPE : ROWS_AFFINE, P.mode_interval ? 0 : 3, 0};
+    const int item = threadIdx.x / TPI, g = threadIdx.x % TPI;
+    const float gam0 = C ? H.layers[0].gamma : 0.f;
+    unsigned int epoch = 0;
+    if (threadIdx.x == 0) s_boxes = 0;
+
+    for (int L = level0; L < kTreeMaxLevels; ++L) {
+        const long long n_in_raw = (long long)*((volatile unsigned long long*)&ws->level_count[L]);
+        if (n_in_raw > B.cap) {  // the previous level overflowed: its nodes were not stored
+            niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+            break;
+        }
+        const long long n_in = n_in_raw;
+        const bool quit = (n_in >= P.thresh) || (L + 1 >= P.n_rounds) || (n_in == 0) || (L + 1 == kTreeMaxLevels);
+        const float* in_lo = B.lvl_lo[L & 1];
+        const float* in_hi = B.lvl_hi[L & 1];
+        float* out_lo = B.lvl_lo[(L + 1) & 1];
+        float* out_hi = B.lvl_hi[(L + 1) & 1];
+        while (true) {
+            __syncthreads();
+            if (threadIdx.x == 0) s_base = (long long)atomicAdd(&ws->grab[L], (unsigned long long)ITEMS);
+            __syncthreads();
+            const long long base = s_base;
+            if (base >= n_in) break;
+            const long long nid = base + item;
+            const bool valid = nid < n_in;
+            // ---- input rows: center and diagonal half extents (src/implicit_function.py:33-37)
+            float* xs = st + item * R * LD;
+            if (g < 4) {
+                const int k = g;
+                for (int r = 0; r < R; ++r) xs[r * LD + k] = 0.f;
+                if (valid && k < 3) {
+                    const float lo = in_lo[3 * nid + k], hi = in_hi[3 * nid + k];
+                    s_lo[item][k] = lo;
+                    s_hi[item][k] = hi;
+                    const float c = __fmul_rn(0.5f, __fadd_rn(lo, hi));
+                    float h = __fsub_rn(hi, c);
+                    if (C) h = fmaxf(__fsub_ru(hi, c), __fsub_ru(c, lo));
+                    xs[k] = c;
+                    if (SLOPE) {
+                        xs[(1 + k) * LD + k] = h;
+                        xs[(5 + k) * LD + k] = C ? __fmul_ru(gam0, h) : 0.f;
+                        xs[4 * LD + k] = C ? __fmul_ru(gam0, fabsf(c)) : 0.f;
+                    } else if (P.mode_interval) {
+                        xs[(R - 1) * LD + k] = C ? __fmaf_ru(gam0, fabsf(c), h) : h;
+                    } else {
+                        xs[(1 + k) * LD + k] = h;
+                        xs[(R - 1) * LD + k] = C ? __fmul_ru(gam0, __fadd_ru(fabsf(c), h)) : 0.f;
+                    }
+                }
+            }
+            __syncthreads();
+            tile_forward<Cfg, C>(H, M.w, sW, sw_cap, resident, plan, st, ob);
+            // ---- consume: one owner lane per item; every lane joins the warp votes
+            int type = -1;
+            if (g == 0 && valid) {
+                float lo, hi;
+                if (SLOPE) slope_out_bounds<C>(ob + item * R, plan.v, lo, hi);
+                else affine_out_bounds<Cfg::R, C>(ob + item * R, plan.v, lo, hi);
+                type = sign_of_bounds(lo, hi, P.offset);
+            }
+            const bool is_unknown = type == NIQ_SIGN_UNKNOWN;
+            const bool is_int = P.with_interior && type == NIQ_SIGN_NEGATIVE;
+            const bool is_ext = P.with_exterior && type == NIQ_SIGN_POSITIVE;
+            const long long pi = niq_warp_reserve(&ws->n_interior, is_int, 1);
+            const long long pe = niq_warp_reserve(&ws->n_exterior, is_ext, 1);
+            const long long pu = quit ? niq_warp_reserve(&ws->n_unknown, is_unknown, 1) : -1;
+            const long long pc = quit ? -1 : niq_warp_reserve(&ws->level_count[L + 1], is_unknown, 2);
+            if (g == 0 && valid) {
+                const float* lo = s_lo[item];
+                const float* hi = s_hi[item];
+                if (is_int) { if (pi < B.cap) put_node(B.res_lo[1], B.res_hi[1], pi, lo, hi); else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY); }
+                if (is_ext) { if (pe < B.cap) put_node(B.res_lo[2], B.res_hi[2], pe, lo, hi); else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY); }
+                if (is_unknown) {
+                    if (quit) {
+                        if (pu < B.cap) put_node(B.res_lo[0], B.res_hi[0], pu, lo, hi);
+                        else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+                    } else if (pc + 1 < B.cap) {
+                        // split along the first longest axis (jnp.argmax: first maximum)
+                        const float e0 = __fsub_rn(hi[0], lo[0]), e1 = __fsub_rn(hi[1], lo[1]), e2 = __fsub_rn(hi[2], lo[2]);
+                        int d = 0;
+                        float em = e0;
+                        if (e1 > em) { d = 1; em = e1; }
+                        if (e2 > em) { d = 2; }
+                        float alo[3] = {lo[0], lo[1], lo[2]}, ahi[3] = {hi[0], hi[1], hi[2]};
+                        float blo[3] = {lo[0], lo[1], lo[2]}, bhi[3] = {hi[0], hi[1], hi[2]};
+                        const float mid = __fmul_rn(0.5f, __fadd_rn(lo[d], hi[d]));
+                        ahi[d] = mid;
+                        blo[d] = mid;
+                        put_node(out_lo, out_hi, pc, alo, ahi);
+                        put_node(out_lo, out_hi, pc + 1, blo, bhi);
+                    } else {
+                        niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+                    }
+                }
+                atomicAdd(&s_boxes, 1ull);
+            }
+        }
+        if (!COOP) {
+            if (threadIdx.x == 0) {
+                if (quit) atomicMax(&ws->last_level, L);
+            }
+            break;
+        }
+        if (quit) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) ws->last_level = L;
+            break;
+        }
+        if (!niq_grid_barrier(&ws->barrier, gridDim.x, epoch, &ws->err)) break;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_boxes) atomicAdd(&ws->n_boxes, s_boxes);
+}
+
+struct TreeLayout {
+    size_t hdr, lvl[2], res[3], total;
+};
+
+static TreeLayout tree_layout(long long cap, int flags) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    TreeLayout L;
+    const size_t nb = al((size_t)cap * 24);  // lower (cap,3) then upper (cap,3)
+    L.hdr = 0;
+    size_t off = al(sizeof(TreeWs));
+    L.lvl[0] = off; off += nb;
+    L.lvl[1] = off; off += nb;
+    L.res[0] = off; off += nb;
+    L.res[1] = off; if (flags & NIQ_TREE_WITH_INTERIOR) off += nb;
+    L.res[2] = off; if (flags & NIQ_TREE_WITH_EXTERIOR) off += nb;
+    L.total = off + 256;
+    return L;
+}
+
+static char* ws_base(void* ws) {
+    return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+}
+
+static void tree_bufs(void* workspace, long long cap, int flags, TreeBufs& B) {
+    const TreeLayout TL = tree_layout(cap, flags);
+    char* base = ws_base(workspace);
+    auto lo = [&](size_t off) { return reinterpret_cast<float*>(base + off); };
+    auto hi = [&](size_t off) { return reinterpret_cast<float*>(base + off + (size_t)cap * 12); };
+    for (int i = 0; i < 2; ++i) { B.lvl_lo[i] = lo(TL.lvl[i]); B.lvl_hi[i] = hi(TL.lvl[i]); }
+    for (int i = 0; i < 3; ++i) { B.res_lo[i] = lo(TL.res[i]); B.res_hi[i] = hi(TL.res[i]); }
+    B.cap = cap;
+}
+
+__global__ void k_tree_finish(TreeWs* ws, long long* counts) {
+    counts[0] = (long long)ws->n_unknown;
+    counts[1] = (long long)ws->n_interior;
+    counts[2] = (long long)ws->n_exterior;
+    counts[3] = (long long)ws->n_boxes;
+}
+
+template <bool COOP>
+static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float* lower, const float* upper,
+                    int split_depth, long long thresh, float offset, int flags, long long cap, long long* counts,
+                    void* workspace, size_t ws_bytes, cudaStream_t s) {
+    NIQ_REQUIRE(m && opts && lower && upper && counts, NIQ_ERR_INVALID_ARG, "null argument");
+    const int mode = opts->mode;
+    NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
+                NIQ_ERR_UNSUPPORTED, "the tree kernels support the interval, affine_fixed and slope_interval modes");
+    NIQ_REQUIRE(split_depth >= 0 || thresh > 0, NIQ_ERR_INVALID_ARG,
+                "must specify at least one of node_terminate_thresh or split_depth as a terminating condition");
+    NIQ_REQUIRE(split_depth < kTreeMaxLevels, NIQ_ERR_INVALID_ARG, "split_depth %d exceeds %d", split_depth, kTreeMaxLevels - 1);
+    NIQ_REQUIRE(cap >= 2, NIQ_ERR_INVALID_ARG, "node capacity too small");
+    const TreeLayout TL = tree_layout(cap, flags);
+    NIQ_REQUIRE(workspace && ws_bytes >= TL.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", TL.total);
+    TreeBufs B;
+    tree_bufs(workspace, cap, flags, B);
+    TreeWs* ws = reinterpret_cast<TreeWs*>(ws_base(workspace));
+    NIQ_CUDA(cudaMemsetAsync(ws, 0, sizeof(TreeWs), s));
+    // root node and level 0 count
+    NIQ_CUDA(cudaMemcpyAsync(B.lvl_lo[0], lower, 12, cudaMemcpyHostToDevice, s));
+    NIQ_CUDA(cudaMemcpyAsync(B.lvl_hi[0], upper, 12, cudaMemcpyHostToDevice, s));
+    const unsigned long long one = 1;
+    NIQ_CUDA(cudaMemcpyAsync(&ws->level_count[0], &one, 8, cudaMemcpyHostToDevice, s));
+    TreeParams P;
+    P.n_rounds = split_depth >= 0 ? split_depth + 1 : kTreeMaxLevels;
+    P.thresh = thresh > 0 ? thresh : (1ll << 62);
+    P.offset = offset;
+    P.with_interior = (flags & NIQ_TREE_WITH_INTERIOR) != 0;
+    P.with_exterior = (flags & NIQ_TREE_WITH_EXTERIOR) != 0;
+    P.mode_interval = mode == NIQ_MODE_INTERVAL;
+    const bool cons = opts->conservative != 0, slope = mode == NIQ_MODE_SLOPE_INTERVAL;
+    const int tpi = tpi_for_width(m->hdr.max_width);
+    int rc = NIQ_OK;
+    auto run = [&](auto kern, int R, int TPIv) -> int {
+        const int items = kNT / TPIv;
+        const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
+        SmemPlan p = plan_smem(state, m->hdr.n_weight_floats, max_layer_floats(m->hdr));
+        NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * m->hdr.max_width, NIQ_ERR_UNSUPPORTED, "shared memory too small");
+        int r2 = prepare_kernel(kern, p.bytes);
+        if (r2) return r2;
+        int per_sm = 0;
+        NIQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kNT, p.bytes));
+        NIQ_REQUIRE(per_sm >= 1, NIQ_ERR_UNSUPPORTED, "tree kernel does not fit on an SM");
+        const int grid = per_sm * device_info().sm_count;
+        NiqModelRef M = m->ref();
+        int level0 = 0;
+        int fixed = p.fixed_floats, cap_ = p.sw_cap, res = p.resident;
+        if (COOP) {
+            void* args[] = {&M, &P, &ws, &B, &level0, &fixed, &cap_, &res};
+            NIQ_CUDA(cudaLaunchCooperativeKernel((const void*)kern, grid, kNT, args, p.bytes, s));
+            return NIQ_OK;
+        }
+        // plain: one launch per level, host reads the next level size (src/kd_tree.py:137-198)
+        for (int L = 0; L < kTreeMaxLevels; ++L) {
+            unsigned long long cnt[2] = {0, 0};
+            NIQ_CUDA(cudaMemcpyAsync(cnt, &ws->level_count[L], 8, cudaMemcpyDeviceToHost, s));
+            NIQ_CUDA(cudaStreamSynchronize(s));
+            const long long n_in = (long long)cnt[0];
+            const bool quit = (n_in >= P.thresh) || (L + 1 >= P.n_rounds) || (n_in == 0) || (L + 1 == kTreeMaxLevels);
+            long long tiles = (n_in + items - 1) / items;
+            int g = (int)(tiles < grid ? (tiles < 1 ? 1 : tiles) : grid);
+            kern<<<g, kNT, p.bytes, s>>>(M, P, ws, B, L, fixed, cap_, res);
+            NIQ_CUDA(cudaGetLastError());
+            if (quit) break;
+        }
+        return NIQ_OK;
+    };
+#define NIQ_TREE(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_tree<TPI, CC, SL, COOP>, SL ? 8 : 5, TPI); })
+    if (slope) { if (cons) { NIQ_TREE(true, true); } else { NIQ_TREE(false, true); } }
+    else { if (cons) { NIQ_TREE(true, false); } else { NIQ_TREE(false, false); } }
+#undef NIQ_TREE
+    if (rc) return rc;
+    k_tree_finish<<<1, 1, 0, s>>>(ws, counts);
+    NIQ_CUDA(cudaGetLastError());
+    int err = 0;
+    NIQ_CUDA(cudaMemcpyAsync(&err, &ws->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    NIQ_REQUIRE(err == 0, err, err == NIQ_ERR_CAPACITY ? "node capacity %lld exceeded" : "tree kernel error (%lld)",
+                err == NIQ_ERR_CAPACITY ? cap : (long long)err);
+    return NIQ_OK;
+}
+
+}  // namespace niq
+
+using namespace niq;
+
+extern "C" {
+
+size_t niq_tree_workspace_size(int64_t node_capacity, int32_t flags) { return tree_layout(node_capacity, flags).total; }
+
+int niq_levelset_tree(const niq_model* model, const niq_bound_opts* opts, const float* lower, const float* upper,
+                      int32_t split_depth, int64_t node_terminate_thresh, float offset, int32_t flags,
+                      int64_t node_capacity, int64_t* counts_out, void* workspace, size_t workspace_bytes,
+                      void* stream) {
+    return run_tree<true>(model, opts, lower, upper, split_depth, node_terminate_thresh, offset, flags, node_capacity,
+                          reinterpret_cast<long long*>(counts_out), workspace, workspace_bytes, as_stream(stream));
+}
+
+int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                            const float* upper, int32_t split_depth, int64_t node_terminate_thresh, float offset,
+                            int32_t flags, int64_t node_capacity, int64_t* counts_out, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+    return run_tree<false>(model, opts, lower, upper, split_depth, node_terminate_thresh, offset, flags, node_capacity,
+                           reinterpret_cast<long long*>(counts_out), workspace, workspace_bytes, as_stream(stream));
+}
+
+int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32_t kind, float** lower, float** upper) {
+    NIQ_REQUIRE(workspace && lower && upper && kind >= 0 && kind <= 2, NIQ_ERR_INVALID_ARG, "bad argument");
+    NIQ_REQUIRE(kind != 1 || (flags & NIQ_TREE_WITH_INTERIOR), NIQ_ERR_INVALID_ARG, "tree built without interior nodes");
+    NIQ_REQUIRE(kind != 2 || (flags & NIQ_TREE_WITH_EXTERIOR), NIQ_ERR_INVALID_ARG, "tree built without exterior nodes");
+    TreeBufs B;
+    tree_bufs(workspace, node_capacity, flags, B);
+    *lower = B.res_lo[kind];
+    *upper = B.res_hi[kind];
+    return NIQ_OK;
+}
+
+}  // extern "C"

@@ -120,3 +120,17 @@ __device__ __forceinline__ long long niq_warp_append(unsigned long long* counter
     base = __shfl_sync(mask, base, leader);
     return (long long)(base + rank);
 }
+
+// Warp-aggregated reservation of `per` consecutive slots for each lane with `want`; all
+// 32 lanes of the warp must call it.  Returns the first slot or -1.
+__device__ __forceinline__ long long niq_warp_reserve(unsigned long long* counter, bool want, int per) {
+    const unsigned int mask = __ballot_sync(0xffffffffu, want);
+    if (!want) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const int rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)(__popc(mask) * per));
+    base = __shfl_sync(mask, base, leader);
+    return (long long)base + (long long)rank * per;
+}

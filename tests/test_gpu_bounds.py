@@ -1,7 +1,9 @@
 """CUDA point evaluation and box bounds against the oracle (oracle/ref_np.py).
 
 Tolerances: point values within 1e-5 relative; reference-arithmetic bounds
-(conservative=False) within 3e-5 of the bound scale max(|lo|,|hi|)+1e-3; conservative
+(conservative=False) within 3e-5 of the bound scale max(|lo|,|hi|)+1e-3 for ReLU and
+1e-4 for TanH/ELU, whose secant slope (f(u)-f(l))/(u-l) amplifies the few-ulp difference
+between CUDA's tanhf/expm1f and NumPy's on narrow boxes; conservative
 bounds contain every FP64 sample of the network inside the box (zero violations) and
 stay within 1e-4 relative width of the FP64 oracle's bounds."""
 import numpy as np
@@ -75,7 +77,7 @@ def test_bounds_match_oracle(niq, R, gpu_ready, mode):
             rlo, rhi = o.bounds_general(params, c, vv)
             scale = np.maximum(np.abs(rlo), np.abs(rhi)) + 1e-3
             err = max(np.max(np.abs(lo - rlo) / scale), np.max(np.abs(hi - rhi) / scale))
-            assert err <= 3e-5, (name, v, err)
+            assert err <= (3e-5 if name.startswith('relu') else 1e-4), (name, v, err)
             rs = R.sign_from_bounds(rlo, rhi)
             near = (np.abs(rlo) < 1e-4 * scale) | (np.abs(rhi) < 1e-4 * scale)
             assert np.all((sign == rs) | near), (name, v)
@@ -92,7 +94,8 @@ def test_bounds_golden(niq, gpu_ready, mode):
             sign, lo, hi = f.bounds_general_box(params, c, vv, offset=0.01)
             glo, ghi = g[f'boxes/{m}/v{v}/{mode}/lower'], g[f'boxes/{m}/v{v}/{mode}/upper']
             scale = np.maximum(np.abs(glo), np.abs(ghi)) + 1e-3
-            assert np.max(np.abs(lo - glo) / scale) <= 3e-5 and np.max(np.abs(hi - ghi) / scale) <= 3e-5, (m, v)
+            tol = 3e-5 if m.startswith('relu') else 1e-4
+            assert np.max(np.abs(lo - glo) / scale) <= tol and np.max(np.abs(hi - ghi) / scale) <= tol, (m, v)
             gs = g[f'boxes/{m}/v{v}/{mode}/sign_off0.01']
             near = (np.abs(glo - 0.01) < 1e-4 * scale) | (np.abs(ghi + 0.01) < 1e-4 * scale)
             assert np.all((sign == gs) | near)

@@ -1,0 +1,245 @@
+"""CUDA queries (cast_rays, level-set tree, HMC, intersection, closest point) against the
+oracle and the golden vectors of the reference.
+
+Decision parity: ray and tree results depend on sign decisions of bounds; a decision
+may differ from the oracle's only where the oracle's bound sits within 1e-5 (relative)
+of the threshold, so ray comparisons allow a small fraction of diverging rays and tree
+comparisons exclude boxes whose oracle bound straddles zero by less than 1e-5."""
+import numpy as np
+import pytest
+
+from conftest import golden, model_from
+
+pytestmark = pytest.mark.gpu
+
+
+def gf(niq, params, mode='affine_fixed', conservative=False, **kw):
+    return niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=conservative, **kw)[0]
+
+
+def ray_match(t, hid, cnt, rt, rhid, rcnt):
+    return (hid == rhid) & (cnt == rcnt) & np.isclose(t, rt, rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize('mode', ['affine_fixed', 'interval', 'slope_interval'])
+def test_cast_rays_golden(niq, R, gpu_ready, mode):
+    g = golden('rays.npz')
+    params = model_from(g, 'model/relu32x3')
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    f = gf(niq, params, mode)
+    t, hid, cnt, nev = niq.queries.cast_rays((f,), (params,), g['rays/roots'], g['rays/dirs'], opts)
+    m = ray_match(t, hid, cnt, g[f'rays/{mode}/t'], g[f'rays/{mode}/hit_id'], g[f'rays/{mode}/count'])
+    assert m.mean() >= 0.97, m.mean()
+
+
+def test_cast_rays_two_functions_golden(niq, gpu_ready):
+    g = golden('rays.npz')
+    p1, p2 = model_from(g, 'model/relu32x3'), model_from(g, 'model/relu16')
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 48
+    opts['n_substeps'] = 2
+    sub = slice(0, g['rays/roots'].shape[0], 3)
+    f = gf(niq, p1)
+    t, hid, cnt, _ = niq.queries.cast_rays((f, f), (p1, p2), g['rays/roots'][sub], g['rays/dirs'][sub], opts)
+    m = ray_match(t, hid, cnt, g['rays2/t'], g['rays2/hit_id'], g['rays2/count'])
+    assert m.mean() >= 0.97, m.mean()
+
+
+@pytest.mark.parametrize('width', [32, 64, 128, 256])
+def test_cast_rays_oracle_and_plain(niq, R, gpu_ready, width):
+    params = niq.workloads.he_mlp([3, width, width, width, 1], 'relu', seed=width, grid=16)
+    roots, dirs = R.generate_camera_rays([0., 0., 3.], [0., 0., -1.], [0., 1., 0.], res=24, fov_deg=60.)
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    f = gf(niq, params)
+    t, hid, cnt, nev = niq.queries.cast_rays((f,), (params,), roots, dirs, opts)
+    tp, hidp, cntp, nevp = niq.queries.cast_rays((f,), (params,), roots, dirs, opts, persistent=False)
+    # the persistent and plain forms run the same per-ray arithmetic
+    np.testing.assert_array_equal(t, tp)
+    np.testing.assert_array_equal(hid, hidp)
+    np.testing.assert_array_equal(cnt, cntp)
+    assert nev == nevp == int(cnt.sum())
+    o = R.generate_implicit(params, 'affine_fixed')
+    rt, rhid, rcnt, _ = R.cast_rays([o], [params], roots, dirs, opts)
+    assert ray_match(t, hid, cnt, rt, rhid, rcnt).mean() >= 0.97
+
+
+def test_cast_rays_conservative_hits(niq, R, gpu_ready):
+    params = niq.workloads.plain_small_model()
+    roots, dirs = R.generate_camera_rays([0., 0., 3.], [0., 0., -1.], [0., 1., 0.], res=32, fov_deg=60.)
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    f = gf(niq, params, conservative=True)
+    t, hid, cnt, _ = niq.queries.cast_rays((f,), (params,), roots, dirs, opts)
+    # every reported hit brackets a sign change of the FP64 network within hit_eps
+    hit = hid > 0
+    p0 = roots[hit].astype(np.float64) + t[hit, None].astype(np.float64) * dirs[hit]
+    p1 = p0 + 1e-3 * dirs[hit]
+    v0, v1 = R.eval_points(params, p0, np.float64), R.eval_points(params, p1, np.float64)
+    assert np.mean(np.sign(v0) != np.sign(v1)) > 0.98
+
+
+def sorted_boxes(lo, hi):
+    a = np.concatenate([np.asarray(lo), np.asarray(hi)], axis=1)
+    return a[np.lexsort(a.T[::-1])] if len(a) else a
+
+
+def box_set_diff(lo, hi, rlo, rhi):
+    A = {tuple(r) for r in np.concatenate([lo, hi], 1).tolist()}
+    B = {tuple(r) for r in np.concatenate([rlo, rhi], 1).tolist()}
+    return A - B, B - A
+
+
+def straddle_ok(R, params, boxes, mode='affine_fixed'):
+    """Boxes whose FP32 oracle bound straddles zero by less than 1e-5 (relative)."""
+    if not boxes:
+        return True
+    b = np.array(sorted(boxes), np.float32)
+    f = R.generate_implicit(params, mode)
+    c = 0.5 * (b[:, :3] + b[:, 3:])
+    v = (b[:, 3:] - c)[:, :, None] * np.eye(3, dtype=np.float32)
+    lo, hi = f.bounds_general(params, c, v)
+    scale = np.maximum(np.abs(lo), np.abs(hi)) + 1e-6
+    return bool(np.all((np.abs(lo) < 1e-5 * scale) | (np.abs(hi) < 1e-5 * scale)))
+
+
+@pytest.mark.parametrize('mode', ['affine_fixed', 'interval'])
+def test_tree_golden(niq, R, gpu_ready, mode):
+    g = golden('tree.npz')
+    params = model_from(g, 'model/relu32x3')
+    f = gf(niq, params, mode)
+    for persistent in (True, False):
+        d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=9,
+                                                                with_interior_nodes=True, with_exterior_nodes=True,
+                                                                persistent=persistent)
+        for kind in ('unknown', 'interior', 'exterior'):
+            extra, missing = box_set_diff(d[f'{kind}_node_lower'], d[f'{kind}_node_upper'],
+                                          g[f'tree/{mode}/{kind}/lower'], g[f'tree/{mode}/{kind}/upper'])
+            assert len(extra) + len(missing) <= 2, (kind, len(extra), len(missing))
+
+
+def test_tree_thresh_golden(niq, gpu_ready):
+    g = golden('tree.npz')
+    params = model_from(g, 'model/relu32x3')
+    f = gf(niq, params)
+    d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3),
+                                                            node_terminate_thresh=200, offset=0.05)
+    extra, missing = box_set_diff(d['unknown_node_lower'], d['unknown_node_upper'], g['tree_thresh/lower'],
+                                  g['tree_thresh/upper'])
+    assert not extra and not missing
+
+
+@pytest.mark.parametrize('conservative', [False, True])
+def test_tree_oracle_spheres(niq, R, gpu_ready, conservative):
+    params = niq.workloads.spheres_sdf_model()
+    f = gf(niq, params, conservative=conservative)
+    d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=12)
+    o = R.generate_implicit(params, 'affine_fixed')
+    r = R.construct_uniform_unknown_levelset_tree(o, params, -np.ones(3), np.ones(3), split_depth=12)
+    extra, missing = box_set_diff(d['unknown_node_lower'], d['unknown_node_upper'], r['unknown_node_lower'],
+                                  r['unknown_node_upper'])
+    # conservative bounds are never narrower: they can only keep more boxes unknown
+    if conservative:
+        assert not missing
+        assert len(extra) <= 0.001 * len(r['unknown_node_lower']) + 2
+    else:
+        assert straddle_ok(R, params, extra | missing)
+
+
+def test_hmc_oracle_and_golden(niq, R, gpu_ready):
+    from oracle import mc_table
+    g = golden('tree.npz')
+    params = model_from(g, 'model/relu32x3')
+    f = gf(niq, params)
+    o = R.generate_implicit(params, 'affine_fixed')
+    T = mc_table.make_table()
+    mc = (T, mc_table.EDGE, mc_table.VERT)
+    for depth, k in ((4, 1), (3, 0), (5, 2)):
+        tris = niq.kd_tree.hierarchical_marching_cubes(f, params, -np.ones(3), np.ones(3), depth, n_subcell_depth=k)
+        rt = R.hierarchical_marching_cubes(o, params, -np.ones(3), np.ones(3), depth, mc, n_subcell_depth=k)
+        assert tris.shape == rt.shape
+        a = np.sort(np.round(tris.reshape(-1, 9), 4), axis=0)
+        b = np.sort(np.round(rt.reshape(-1, 9), 4), axis=0)
+        assert np.max(np.abs(a - b)) < 1e-3
+        key = f'hmc/d{depth}s{k}/tris'
+        if key in g:
+            ref = g[key]
+            assert ref.shape == tris.shape
+            # same crossing vertices and the same total vector area (triangulation-invariant)
+            va = np.unique(np.round(tris.reshape(-1, 3), 4), axis=0)
+            vb = np.unique(np.round(ref.reshape(-1, 3), 4), axis=0)
+            assert va.shape == vb.shape and np.max(np.abs(va - vb)) < 1e-3
+            area = lambda x: 0.5 * np.cross(x[:, 1] - x[:, 0], x[:, 2] - x[:, 0]).sum(0)
+            np.testing.assert_allclose(area(tris), area(ref), atol=1e-4)
+
+
+@pytest.mark.parametrize('mode', ['affine_all', 'affine_fixed'])
+def test_intersection_golden(niq, gpu_ready, mode):
+    g = golden('queries.npz')
+    A = model_from(g, 'model/A')
+    for name in ('near', 'far'):
+        Bp = model_from(g, f'model/B_{name}')
+        fa, fb = gf(niq, A, mode), gf(niq, Bp, mode)
+        found, ia, ib, loc = niq.kd_tree.find_any_intersection((fa, fb), (A, Bp), -np.ones(3), np.ones(3), 0.02)
+        assert found == bool(g[f'isect/{name}/{mode}/found']), name
+        if found:
+            va = niq.implicit_mlp_utils.generate_implicit_from_params(A, 'affine_fixed')[0](A, loc)
+            vb = niq.implicit_mlp_utils.generate_implicit_from_params(Bp, 'affine_fixed')[0](Bp, loc)
+            assert va < 0.05 and vb < 0.05
+
+
+def test_intersection_persistent_vs_plain(niq, gpu_ready):
+    g = golden('queries.npz')
+    A = model_from(g, 'model/A')
+    for name in ('near', 'far'):
+        Bp = model_from(g, f'model/B_{name}')
+        r1 = niq.kd_tree.find_any_intersection((gf(niq, A), gf(niq, Bp)), (A, Bp), -np.ones(3), np.ones(3), 0.02)
+        # affine_truncate runs the plain host loop of the growing-term engine
+        ft = dict(affine_n_truncate=64, affine_truncate_policy='absolute')
+        r2 = niq.kd_tree.find_any_intersection((gf(niq, A, 'affine_truncate', **ft), gf(niq, Bp, 'affine_truncate', **ft)),
+                                               (A, Bp), -np.ones(3), np.ones(3), 0.02)
+        assert r1[0] == r2[0]
+
+
+def test_closest_point_golden(niq, R, gpu_ready):
+    g = golden('queries.npz')
+    A = model_from(g, 'model/A')
+    f = gf(niq, A)
+    q = g['cp/q']
+    for B in (8, 2048):
+        dist, loc = niq.kd_tree.closest_point(f, A, -np.ones(3), np.ones(3), q, eps=0.05, batch_process_size=B)
+        rd, rl = g[f'cp/B{B}/dist'], g[f'cp/B{B}/loc']
+        fin = np.isfinite(rd)
+        assert np.array_equal(np.isfinite(dist), fin)
+        close = np.isclose(dist[fin], rd[fin], rtol=1e-4, atol=1e-5)
+        assert close.mean() >= 0.9, close.mean()
+        o = R.generate_implicit(A, 'affine_fixed')
+        od, ol = R.closest_point(o, A, -np.ones(3), np.ones(3), q, eps=0.05, batch_process_size=B)
+        assert np.isclose(dist[fin], od[fin], rtol=1e-4, atol=1e-5).mean() >= 0.9
+
+
+def test_closest_point_persistent_and_batched(niq, R, gpu_ready):
+    params = niq.workloads.spheres_sdf_model()
+    f = gf(niq, params, conservative=True)
+    rng = np.random.default_rng(3)
+    q = rng.uniform(-1.2, 1.2, (300, 3)).astype(np.float32)
+    eps = 1e-3
+    d_ref, l_ref = niq.kd_tree.closest_point(f, params, -np.ones(3), np.ones(3), q, eps=eps)
+    d_p, l_p = niq.kd_tree.closest_point(f, params, -np.ones(3), np.ones(3), q, eps=eps, persistent=True)
+    fin = np.isfinite(d_ref)
+    assert np.array_equal(fin, np.isfinite(d_p))
+    # both are upper bounds built from eps-small nodes: they agree within ~2 leaf diagonals
+    assert np.all(np.abs(d_p[fin] - d_ref[fin]) <= 2 * eps + 1e-5)
+    # the true distance to the spheres surface is below both
+    cen, rad = niq.workloads.spheres_scene()
+    true = np.abs(niq.workloads.spheres_sdf(q.astype(np.float64), cen, rad))
+    assert np.mean(d_p[fin] >= true[fin] - 0.05) > 0.95
+    # the batched form over a model table returns the persistent form's results
+    other = niq.workloads.he_mlp([3, 48, 48, 1], 'tanh', seed=9, grid=16)
+    out = niq.batched.closest_point_many(f, [params, other], [0, 1, 0], [q[:100], q[100:200], q[200:]],
+                                         -np.ones(3), np.ones(3), eps)
+    np.testing.assert_array_equal(out[0][0], d_p[:100])
+    np.testing.assert_array_equal(out[2][0], d_p[200:])
+    d_o, _ = niq.kd_tree.closest_point(f, other, -np.ones(3), np.ones(3), q[100:200], eps=eps, persistent=True)
+    np.testing.assert_array_equal(out[1][0], d_o)
