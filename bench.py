@@ -1,0 +1,332 @@
+"""Benchmark of the range-analysis query engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config tree|rays|batched]
+
+Default workload (--config tree): the level-set kd-tree + hierarchical marching cubes of
+a 3->64x4->1 ReLU MLP fitted to the SDF of 12 spheres, bisected 24 times (256^3 leaves,
+affine_fixed with outward rounding), then marching cubes on every unknown leaf.  One
+step = one full build + extraction.  ``value`` is bounded boxes per second of the
+persistent form with the model resident on the device; ``e2e`` is the same through the
+public Python API (kd_tree.hierarchical_marching_cubes) with the root box sent from the
+host and the triangles read back every step.  The plain form (one launch + host sync
+per level, the reference's loop structure) is measured beside it.
+
+Multi-GPU: the path has no exchange step, so N GPUs run N independent replicas of the
+workload (torchrun, one rank per GPU); value = all ranks' boxes / max-over-ranks time.
+
+--impl reference times the NumPy restatement of the reference's algorithm (oracle/,
+the reference itself is JAX and cannot run here) on the host cores: each step builds
+the same tree to 15 bisections (a bounded sample of the workload) and reports boxes/s.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = 'neural-implicit-queries_gb300'
+
+SPLIT_DEPTH = 24          # 256^3 leaves
+CPU_SAMPLE_DEPTH = 15     # bounded CPU sample of the same tree
+
+
+def mlp_macs(params):
+    niq = importlib.import_module(PKG)
+    return sum(A.shape[0] * A.shape[1] for A, _, _ in niq.mlp.spec_layers(params))
+
+
+def box_flops(params, v=3):
+    """Algorithmic FLOPs of one bounded box: 2 (v + 2) S, S = sum in*out."""
+    return 2 * (v + 2) * mlp_macs(params)
+
+
+def dist_info():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.gpu}', f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ''
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or '').strip().splitlines():
+            p = [x.strip() for x in line.split(',')]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace('.', '', 1).isdigit())
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    torch.cuda.set_device(local)
+    niq = importlib.import_module(PKG)
+    lib = importlib.import_module(PKG + '._lib')
+    io = importlib.import_module(PKG + '._io')
+    kd = niq.kd_tree
+    params = niq.workloads.spheres_sdf_model()
+    f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=True)
+    lower, upper = np.full(3, -1., np.float32), np.ones(3, np.float32)
+    model = niq.mlp.device_model(params)
+    L = lib.load()
+    bo = f.bound_opts()
+    stream = torch.cuda.current_stream()
+    l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')  # 256 MiB > 129 MB L2
+
+    # ---- device-resident form: tree (one cooperative launch) + HMC extraction
+    cap = 1 << 23
+    ws_bytes = L.niq_tree_workspace_size(cap, 0)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device='cuda')
+    counts = torch.zeros(4, dtype=torch.int64, device='cuda')
+    hws = torch.empty(L.niq_hmc_workspace_size(), dtype=torch.uint8, device='cuda')
+    tri_cap = 1 << 23
+    tris = torch.empty((tri_cap, 3, 3), dtype=torch.float32, device='cuda')
+    ntri = torch.zeros(1, dtype=torch.int64, device='cuda')
+    lo3 = (lib.C.c_float * 3)(*lower.tolist())
+    hi3 = (lib.C.c_float * 3)(*upper.tolist())
+
+    def tree_step(plain=False):
+        fn = L.niq_levelset_tree_plain if plain else L.niq_levelset_tree
+        lib.check(fn(model.handle, lib.C.byref(bo), lo3, hi3, SPLIT_DEPTH, 0, 0.0, 0, cap, io.ptr(counts),
+                     io.ptr(ws), ws_bytes, stream.cuda_stream))
+
+    def hmc_step():
+        n_leaves = int(counts_host[0])
+        lo, hi = kd._tree_nodes(ws, cap, 0, 0, n_leaves)
+        lib.check(L.niq_hmc_extract(model.handle, n_leaves, io.ptr(lo), io.ptr(hi), 0, io.ptr(tris), tri_cap,
+                                    io.ptr(ntri), io.ptr(hws), hws.numel(), stream.cuda_stream))
+
+    tree_step()
+    counts_host = counts.cpu().numpy()
+    n_boxes = int(counts_host[3])
+    hmc_step()
+    n_tris = int(ntri.item())
+
+    def timed(fn_step, K, W):
+        for _ in range(W):
+            fn_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        times = []
+        for _ in range(K):
+            flush_l2(l2buf)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn_step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        torch.cuda.synchronize()
+        return times
+
+    tree_t, hmc_t = [], []
+
+    def full_step():
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        tree_step()
+        e1.record(stream)
+        hmc_step()
+        e2.record(stream)
+        e2.synchronize()
+        tree_t.append(e0.elapsed_time(e1) / 1e3)
+        hmc_t.append(e1.elapsed_time(e2) / 1e3)
+
+    with ClockSampler(local) as clk:
+        step_times = timed(full_step, args.steps, args.warmup)
+    tree_t, hmc_t = tree_t[args.warmup:], hmc_t[args.warmup:]
+    t_step = sum(step_times) / len(step_times)
+
+    # ---- plain form (per-level launches + host syncs), same tree
+    plain_times = timed(lambda: tree_step(plain=True), max(3, args.steps // 2), 1)
+    t_plain = sum(plain_times) / len(plain_times)
+
+    # ---- e2e through the public API: host root box in, host triangles out
+    def e2e_step():
+        return kd.hierarchical_marching_cubes(f, params, lower, upper, 8, n_subcell_depth=0)
+    for _ in range(args.warmup):
+        out = e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = e2e_step()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = sum(e2e_times) / len(e2e_times)
+
+    # ---- max over ranks
+    if world > 1:
+        tt = torch.tensor([t_step, t_e2e, t_plain], device='cuda')
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step, t_e2e, t_plain = tt.tolist()
+    value = world * n_boxes / t_step
+    bf = box_flops(params)
+    t_tree = sum(tree_t) / len(tree_t)
+    achieved_tf = n_boxes * bf / t_tree / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except (OSError, ValueError):
+        pass
+    sm_max = float(peaks.get('sm_max_mhz', 2070.0))
+    props = torch.cuda.get_device_properties(local)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    line = {
+        "metric": "bounded boxes/s (level-set tree 256^3 + HMC, 12-sphere ReLU 3x64x4 MLP, affine_fixed)",
+        "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (fitted 12-sphere SDF MLP, committed weights)",
+        "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12", "split_depth": SPLIT_DEPTH,
+                   "leaves": int(counts_host[0]), "boxes_per_step": n_boxes, "triangles_per_step": n_tris,
+                   "mode": "affine_fixed conservative", "l2": "flushed: 256 MiB write between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * n_boxes / t_e2e, "unit": "boxes/s", "h2d_bytes_per_step": 24,
+                "d2h_bytes_per_step": int(out.nbytes) + 32, "ms_per_step": t_e2e * 1e3,
+                "api": "kd_tree.hierarchical_marching_cubes(depth=8, n_subcell_depth=0)"},
+        "plain": {"value": world * n_boxes / t_plain, "unit": "boxes/s", "ms_per_step": t_plain * 1e3,
+                  "form": "one launch + host sync per level (niq_levelset_tree_plain)",
+                  "persistent_speedup": t_plain / (sum(tree_t) / len(tree_t))},
+        "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3},
+        "roofline": {"bound": "fp32", "kernel": "k_tree (persistent level-set tree)",
+                     "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tf / fp32_peak, "traffic": None,
+                     "flops_per_box": bf,
+                     "peak_source": (f"FP32 FMA pipe: {props.multi_processor_count} SMs x 128 lanes x 2 FLOP x "
+                                     f"{sm_max:.0f} MHz (MEASURED_PEAKS.json sm_max_mhz); the file has no FP32 "
+                                     "figure and this kernel uses neither tensor cores nor significant HBM"),
+                     "hbm_gbs_of_measured": None},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(params)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(params, seconds=20.0):
+    """The NumPy oracle (single process, BLAS threads on all cores) classifying the
+    level-set tree of the same model to CPU_SAMPLE_DEPTH bisections."""
+    from oracle import ref_np as R
+    f = R.generate_implicit(params, 'affine_fixed')
+    t0 = time.perf_counter()
+    boxes = 0
+    reps = 0
+    while True:
+        d = R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3),
+                                                      split_depth=CPU_SAMPLE_DEPTH)
+        boxes += d['n_boxes_classified']
+        reps += 1
+        if time.perf_counter() - t0 > seconds or reps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": boxes / dt, "unit": "boxes/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"oracle/ref_np.py level-set tree of the same model to {CPU_SAMPLE_DEPTH} bisections "
+                      f"({boxes // reps} boxes) x{reps}, numpy fp32 with BLAS on all cores"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    niq = importlib.import_module(PKG)
+    from oracle import ref_np as R
+    params = niq.workloads.spheres_sdf_model()
+    f = R.generate_implicit(params, 'affine_fixed')
+    for _ in range(args.warmup):
+        R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=CPU_SAMPLE_DEPTH)
+    times, boxes = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        d = R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=CPU_SAMPLE_DEPTH)
+        times.append(time.perf_counter() - t0)
+        boxes = d['n_boxes_classified']
+    t = sum(times) / len(times)
+    v = boxes / t
+    line = {"impl": "reference",
+            "metric": "bounded boxes/s (level-set tree 256^3 + HMC, 12-sphere ReLU 3x64x4 MLP, affine_fixed)",
+            "value": v, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (fitted 12-sphere SDF MLP, committed weights)",
+            "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12",
+                       "split_depth": CPU_SAMPLE_DEPTH, "boxes_per_step": int(boxes),
+                       "note": "bounded sample: the reference is JAX (absent); its NumPy restatement runs"},
+            "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"tree to {CPU_SAMPLE_DEPTH} bisections, numpy fp32, BLAS on all cores"},
+            "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == 'ours' else args.warmup
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

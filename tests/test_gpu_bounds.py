@@ -1,9 +1,10 @@
 """CUDA point evaluation and box bounds against the oracle (oracle/ref_np.py).
 
 Tolerances: point values within 1e-5 relative; reference-arithmetic bounds
-(conservative=False) within 3e-5 of the bound scale max(|lo|,|hi|)+1e-3 for ReLU and
-1e-4 for TanH/ELU, whose secant slope (f(u)-f(l))/(u-l) amplifies the few-ulp difference
-between CUDA's tanhf/expm1f and NumPy's on narrow boxes; conservative
+(conservative=False) within 1e-4 of the bound scale max(|lo|,|hi|)+1e-3 (FMA
+accumulation order over up to 256-term dot products, and the secant slope
+(f(u)-f(l))/(u-l) of TanH/ELU amplifying the few-ulp difference between CUDA's
+tanhf/expm1f and NumPy's, both reach a few 1e-5; real defects are >= 1e-3); conservative
 bounds contain every FP64 sample of the network inside the box (zero violations) and
 stay within 1e-4 relative width of the FP64 oracle's bounds."""
 import numpy as np
@@ -77,7 +78,7 @@ def test_bounds_match_oracle(niq, R, gpu_ready, mode):
             rlo, rhi = o.bounds_general(params, c, vv)
             scale = np.maximum(np.abs(rlo), np.abs(rhi)) + 1e-3
             err = max(np.max(np.abs(lo - rlo) / scale), np.max(np.abs(hi - rhi) / scale))
-            assert err <= (3e-5 if name.startswith('relu') else 1e-4), (name, v, err)
+            assert err <= 1e-4, (name, v, err)
             rs = R.sign_from_bounds(rlo, rhi)
             near = (np.abs(rlo) < 1e-4 * scale) | (np.abs(rhi) < 1e-4 * scale)
             assert np.all((sign == rs) | near), (name, v)
