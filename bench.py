@@ -139,7 +139,7 @@ def run_ours(args):
 
     def tree_step(plain=False):
         fn = L.niq_levelset_tree_plain if plain else L.niq_levelset_tree
-        lib.check(fn(model.handle, lib.C.byref(bo), lo3, hi3, SPLIT_DEPTH, 0, 0.0, 0, cap, io.ptr(counts),
+        lib.check(fn(model.handle, lib.C.byref(bo), lo3, hi3, args.split_depth, 0, 0.0, 0, cap, io.ptr(counts),
                      io.ptr(ws), ws_bytes, stream.cuda_stream))
 
     def hmc_step():
@@ -189,6 +189,9 @@ def run_ours(args):
         step_times = timed(full_step, args.steps, args.warmup)
     tree_t, hmc_t = tree_t[args.warmup:], hmc_t[args.warmup:]
     t_step = sum(step_times) / len(step_times)
+    if args.quick:   # profiling runs: the timed steps only
+        print(json.dumps({"quick": True, "ms_per_step": t_step * 1e3, "boxes": n_boxes}))
+        return
 
     # ---- plain form (per-level launches + host syncs), same tree
     plain_times = timed(lambda: tree_step(plain=True), max(3, args.steps // 2), 1)
@@ -196,7 +199,7 @@ def run_ours(args):
 
     # ---- e2e through the public API: host root box in, host triangles out
     def e2e_step():
-        return kd.hierarchical_marching_cubes(f, params, lower, upper, 8, n_subcell_depth=0)
+        return kd.hierarchical_marching_cubes(f, params, lower, upper, args.split_depth // 3, n_subcell_depth=0)
     for _ in range(args.warmup):
         out = e2e_step()
     torch.cuda.synchronize()
@@ -232,7 +235,7 @@ def run_ours(args):
         "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (fitted 12-sphere SDF MLP, committed weights)",
-        "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12", "split_depth": SPLIT_DEPTH,
+        "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12", "split_depth": args.split_depth,
                    "leaves": int(counts_host[0]), "boxes_per_step": n_boxes, "triangles_per_step": n_tris,
                    "mode": "affine_fixed conservative", "l2": "flushed: 256 MiB write between timed steps",
                    "parallelism": f"replicas x{world}"},
@@ -320,6 +323,8 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--split-depth', type=int, default=SPLIT_DEPTH, help='bisections of the tree (24: 256^3 leaves)')
+    ap.add_argument('--quick', action='store_true', help='timed steps only (for profiler runs)')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == 'ours' else args.warmup
     if args.impl == 'reference':

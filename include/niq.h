@@ -213,14 +213,17 @@ int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* o
 /* ---- many models in one launch (closest point over a model table) ------------------ *
  * Job j runs query_count[j] closest-point queries starting at row query_offset[j] of
  * query_points against models[job_model[j]]; all jobs run in one persistent launch.
- * Arrays job_model/query_offset/query_count are host arrays of n_jobs entries. */
+ * Arrays job_model/query_offset/query_count are host arrays of n_jobs entries.
+ * status_out: optional device int32; when given the call does not sync and the
+ * traversal's status (NIQ_OK or NIQ_ERR_CAPACITY) is written there; when NULL the call
+ * syncs the stream and returns that status. */
 size_t niq_batched_closest_point_workspace_size(int64_t total_queries, int32_t n_jobs);
 int niq_batched_closest_point(const niq_model* const* models, int32_t n_models,
                               const niq_bound_opts* opts, int32_t n_jobs,
                               const int32_t* job_model, const int64_t* query_offset,
                               const int64_t* query_count, const float* query_points,
                               const float* lower, const float* upper, float eps,
-                              float* min_dist_out, float* min_loc_out,
+                              float* min_dist_out, float* min_loc_out, int32_t* status_out,
                               void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus

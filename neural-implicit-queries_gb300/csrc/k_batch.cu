@@ -186,7 +186,13 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
                     for (int k = 0; k < 3; ++k) s_loc[item][k] = c[k];
                 }
             }
-            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && cd < s_best[item]) {
+            // prune with the query-to-box distance, a true lower bound (see k_search.cu)
+            float bd2 = 0.f;
+            for (int k = 0; k < 3; ++k) {
+                const float dd = fmaxf(fmaxf(__fsub_rd(lo[k], q[k]), __fsub_rd(q[k], hi[k])), 0.f);
+                bd2 = __fmaf_rd(dd, dd, bd2);
+            }
+            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && __fsqrt_rd(bd2) < s_best[item]) {
                 const int t = s_top[item];
                 if (t + 2 <= kBStack) {
                     int d = 0;
@@ -265,8 +271,8 @@ size_t niq_batched_closest_point_workspace_size(int64_t total_queries, int32_t n
 int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, const niq_bound_opts* opts,
                               int32_t n_jobs, const int32_t* job_model, const int64_t* query_offset,
                               const int64_t* query_count, const float* query_points, const float* lower,
-                              const float* upper, float eps, float* min_dist_out, float* min_loc_out, void* workspace,
-                              size_t workspace_bytes, void* stream) {
+                              const float* upper, float eps, float* min_dist_out, float* min_loc_out,
+                              int32_t* status_out, void* workspace, size_t workspace_bytes, void* stream) {
     NIQ_REQUIRE(models && opts && lower && upper && n_models >= 1 && n_jobs >= 0, NIQ_ERR_INVALID_ARG, "bad argument");
     NIQ_REQUIRE(opts->mode == NIQ_MODE_AFFINE_FIXED || opts->mode == NIQ_MODE_INTERVAL ||
                     opts->mode == NIQ_MODE_SLOPE_INTERVAL,
@@ -328,6 +334,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     float* stacks = reinterpret_cast<float*>(b + off);
     NIQ_REQUIRE(off + slots_max() * kBStack * 24 <= workspace_bytes - 256, NIQ_ERR_CAPACITY, "workspace too small");
     NIQ_CUDA(cudaMemsetAsync(b, 0, 64, s));
+    if (status_out) NIQ_CUDA(cudaMemsetAsync(status_out, 0, 4, s));
     if (n_chunks == 0) return NIQ_OK;
     // host staging: these copies are synchronous w.r.t. the host buffers (pageable memory)
     NIQ_CUDA(cudaMemcpyAsync(d_chunks, sorted.data(), n_chunks * sizeof(BChunk), cudaMemcpyHostToDevice, s));
@@ -345,7 +352,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
     a.stacks = stacks;
     a.next_chunk = next;
-    a.err = err;
+    a.err = status_out ? reinterpret_cast<int*>(status_out) : err;
     const size_t smem = kSmemBudget;
     a.smem_floats = (int)(smem / 4);
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
@@ -364,6 +371,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     if (slope) rc = cons ? run(k_batched_cp<true, true>) : run(k_batched_cp<false, true>);
     else rc = cons ? run(k_batched_cp<true, false>) : run(k_batched_cp<false, false>);
     if (rc) return rc;
+    if (status_out) return NIQ_OK;
     int e = 0;
     NIQ_CUDA(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
     NIQ_CUDA(cudaStreamSynchronize(s));

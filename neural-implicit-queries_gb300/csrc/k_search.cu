@@ -76,6 +76,16 @@ __device__ __forceinline__ float norm3(float a, float b, float c) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c)));
 }
 
+// Distance from q to the box [lo, hi], rounded down (a lower bound).
+__device__ __forceinline__ float box_dist(const float* q, const float* lo, const float* hi) {
+    float s = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        const float d = fmaxf(fmaxf(__fsub_rd(lo[k], q[k]), __fsub_rd(q[k], hi[k])), 0.f);
+        s = __fmaf_rd(d, d, s);
+    }
+    return __fsqrt_rd(s);
+}
+
 // ======================================================================== closest point
 struct CpArgs {
     const float* q;          // (Q,3)
@@ -332,7 +342,11 @@ __global__ void __launch_bounds__(kNT) k_cp_persistent(NiqModelRef M, CpArgs a, 
                     for (int k = 0; k < 3; ++k) s_loc[item][k] = c[k];
                 }
             }
-            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && cd < s_best[item]) {
+            // prune with the distance from the query to the box: a true lower bound on every
+            // candidate inside it (the reference computes it, src/kd_tree.py:699, but prunes
+            // with the center distance, which under depth-first order would drop subtrees
+            // that hold the closest candidate)
+            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && box_dist(q, lo, hi) < s_best[item]) {
                 const int t = s_top[item];
                 if (t + 2 <= kCpStack) {
                     const int d = first_longest(lo, hi);

@@ -30,14 +30,16 @@ def _common_opts(funcs_tuple):
     return funcs_tuple[0].bound_opts()
 
 
-def cast_rays(funcs_tuple, params_tuple, roots, dirs, opts, persistent=True):
+def cast_rays(funcs_tuple, params_tuple, roots, dirs, opts, persistent=True, return_device=False):
     """src/queries.py:134-175: returns ``(t, hit_id, count, N_evals)``.
 
     ``t`` is the start of the step at termination, ``hit_id`` the 1-based index of the
     function whose sign changed (0: none), ``count`` the steps taken.  ``N_evals`` counts
     the ray-steps actually evaluated (the reference also counts its bucket padding).
     ``persistent=False`` runs the plain form: one launch, one device-to-host sync and one
-    compaction per iteration, as the reference's loop does."""
+    compaction per iteration, as the reference's loop does.  ``return_device=True``
+    returns CUDA tensors (``N_evals`` as a one-element tensor per function) without
+    synchronising the stream."""
     if not isinstance(funcs_tuple, (tuple, list)):
         funcs_tuple, params_tuple = (funcs_tuple,), (params_tuple,)
     if len(funcs_tuple) != len(params_tuple):
@@ -62,5 +64,7 @@ def cast_rays(funcs_tuple, params_tuple, roots, dirs, opts, persistent=True):
     _lib.check(fn(handles, len(models), _lib.C.byref(bo), n, _io.ptr(rt), _io.ptr(dt), _lib.C.byref(co),
                   _io.ptr(t_out), _io.ptr(hit), _io.ptr(cnt), _io.ptr(nev), _io.ptr(ws), ws_bytes,
                   _io.stream_handle()))
+    if return_device:
+        return t_out, hit, cnt, nev
     n_evals = int(nev[0].item()) if n else 0
     return _io.back(t_out, kind), _io.back(hit, kind), _io.back(cnt, kind), n_evals

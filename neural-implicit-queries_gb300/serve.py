@@ -1,0 +1,270 @@
+"""A request loop over resident models: continuous batching of range-analysis queries.
+
+The reference has no serving path; this module turns the query kernels into a service.
+Models stay resident on the device (one packed blob each).  Requests of three kinds
+arrive from any thread:
+
+* ``RayRequest``: cast a tile of rays against one model (queries.cast_rays),
+* ``ClosestRequest``: closest points of a query batch on one model
+  (kd_tree.closest_point, persistent per-query traversal),
+* ``IntersectRequest``: does model A, moved by a rigid transform, meet model B
+  (kd_tree.find_any_intersection)?
+
+A scheduler thread admits queued requests while their estimated device memory fits the
+budget, groups every admitted closest-point request of an admission wave into one
+multi-model launch (batched.closest_point_packed), and issues each group on one of a
+pool of CUDA streams, so work admitted later overlaps work already on the device.  A
+completion thread polls the streams' events, copies results to the host and resolves
+the request futures; latency is measured from submission to resolution.
+"""
+from __future__ import annotations
+
+import collections
+import dataclasses
+import queue
+import threading
+import time
+from concurrent.futures import Future
+
+import numpy as np
+
+from . import _io, _lib, batched, kd_tree, queries
+from .implicit_mlp_utils import generate_implicit_from_params
+from .mlp import device_model, prepend_op, spatial_transformation
+
+
+@dataclasses.dataclass
+class RayRequest:
+    model: int
+    roots: np.ndarray
+    dirs: np.ndarray
+    opts: dict = None
+
+
+@dataclasses.dataclass
+class ClosestRequest:
+    model: int
+    points: np.ndarray
+    eps: float = 1e-3
+
+
+@dataclasses.dataclass
+class IntersectRequest:
+    model_a: int
+    model_b: int
+    R: np.ndarray
+    t: np.ndarray
+    eps: float = 1e-3
+
+
+@dataclasses.dataclass
+class _Pending:
+    req: object
+    future: Future
+    t_submit: float
+    bytes: int
+
+
+def estimate_bytes(req):
+    """Device memory a request holds while in flight (inputs, outputs, workspace)."""
+    if isinstance(req, RayRequest):
+        n = len(req.roots)
+        return 24 * n + 12 * n + 28 * n + 4096
+    if isinstance(req, ClosestRequest):
+        return 12 * len(req.points) + 16 * len(req.points) + 4096
+    return (1 << 20) * 12 * 8   # intersection: node arrays for 1M nodes per level, 4 levels buffers
+
+
+class Server:
+    def __init__(self, params_list, mode='affine_fixed', budget_bytes=40 << 30, n_streams=4, lower=(-1., -1., -1.),
+                 upper=(1., 1., 1.), conservative=True):
+        import torch
+        self.torch = torch
+        self.params = list(params_list)
+        self.func, _ = generate_implicit_from_params(self.params[0], mode, conservative=conservative)
+        self.table = batched.ModelTable(self.params)
+        self.lower = np.asarray(lower, np.float32)
+        self.upper = np.asarray(upper, np.float32)
+        self.budget = int(budget_bytes)
+        self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
+        self._rr = 0
+        self._q = queue.Queue()
+        self._inflight = collections.deque()
+        self._inflight_bytes = 0
+        self._lock = threading.Condition()
+        self._stop = False
+        self.latencies = []
+        self.completed = 0
+        self._sched = threading.Thread(target=self._schedule, daemon=True)
+        self._done = threading.Thread(target=self._complete, daemon=True)
+        self._device = torch.cuda.current_device()
+        self._sched.start()
+        self._done.start()
+
+    # ------------------------------------------------------------------ client side
+    def submit(self, req):
+        fut = Future()
+        self._q.put(_Pending(req, fut, time.perf_counter(), estimate_bytes(req)))
+        return fut
+
+    def close(self):
+        with self._lock:
+            self._stop = True
+            self._lock.notify_all()
+        self._q.put(None)
+        self._sched.join()
+        self._done.join()
+
+    def stats(self):
+        lat = np.array(self.latencies) * 1e3
+        if lat.size == 0:
+            return {"completed": 0}
+        return {"completed": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean())}
+
+    # ------------------------------------------------------------------ scheduler
+    def _next_stream(self):
+        s = self.streams[self._rr % len(self.streams)]
+        self._rr += 1
+        return s
+
+    def _schedule(self):
+        torch = self.torch
+        torch.cuda.set_device(self._device)
+        waiting = collections.deque()
+        while True:
+            # drain the queue without blocking when work is waiting for admission
+            try:
+                item = self._q.get(timeout=0.0005 if waiting else None)
+                if item is None:
+                    if not waiting:
+                        break
+                else:
+                    waiting.append(item)
+                    while True:
+                        try:
+                            nxt = self._q.get_nowait()
+                        except queue.Empty:
+                            break
+                        if nxt is None:
+                            self._q.put(None)
+                            break
+                        waiting.append(nxt)
+            except queue.Empty:
+                pass
+            # admission wave: everything that fits the budget right now
+            wave = []
+            with self._lock:
+                while waiting and self._inflight_bytes + waiting[0].bytes <= self.budget:
+                    p = waiting.popleft()
+                    self._inflight_bytes += p.bytes
+                    wave.append(p)
+                if not wave and waiting and self._inflight_bytes == 0:
+                    p = waiting.popleft()   # larger than the whole budget: run it alone
+                    self._inflight_bytes += p.bytes
+                    wave.append(p)
+            if wave:
+                self._launch(wave)
+            elif waiting:
+                with self._lock:
+                    self._lock.wait(timeout=0.001)
+            if self._stop and not waiting and self._q.empty():
+                break
+        with self._lock:
+            self._inflight.append(None)
+            self._lock.notify_all()
+
+    def _launch(self, wave):
+        torch = self.torch
+        cps = [p for p in wave if isinstance(p.req, ClosestRequest)]
+        rest = [p for p in wave if not isinstance(p.req, ClosestRequest)]
+        if cps:
+            s = self._next_stream()
+            with torch.cuda.stream(s):
+                counts = np.array([len(p.req.points) for p in cps], np.int64)
+                offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+                pts = np.concatenate([np.asarray(p.req.points, np.float32).reshape(-1, 3) for p in cps])
+                eps = cps[0].req.eps
+                dist, loc = batched.closest_point_packed(self.func, self.table, [p.req.model for p in cps], offs,
+                                                         counts, pts, self.lower, self.upper, eps)
+                ev = torch.cuda.Event()
+                ev.record(s)
+            self._push(('closest', cps, (dist, loc, offs, counts), ev))
+        for p in rest:
+            s = self._next_stream()
+            with torch.cuda.stream(s):
+                if isinstance(p.req, RayRequest):
+                    opts = p.req.opts or queries.get_default_cast_opts()
+                    m = p.req.model
+                    t, hid, cnt, _ = queries.cast_rays((self.func,), (self.params[m],),
+                                                       torch.from_numpy(np.asarray(p.req.roots, np.float32)).cuda(),
+                                                       torch.from_numpy(np.asarray(p.req.dirs, np.float32)).cuda(), opts)
+                    out = (t, hid, cnt)
+                else:
+                    pa = prepend_op(self.params[p.req.model_a], spatial_transformation())
+                    pa['0000.spatial_transformation.R'] = np.asarray(p.req.R, np.float32)
+                    pa['0000.spatial_transformation.t'] = np.asarray(p.req.t, np.float32)
+                    pb = prepend_op(self.params[p.req.model_b], spatial_transformation())
+                    found = kd_tree.find_any_intersection((self.func, self.func), (pa, pb), self.lower, self.upper,
+                                                          p.req.eps)
+                    out = found
+                ev = torch.cuda.Event()
+                ev.record(s)
+            self._push(('single', [p], out, ev))
+
+    def _push(self, rec):
+        with self._lock:
+            self._inflight.append(rec)
+            self._lock.notify_all()
+
+    # ------------------------------------------------------------------ completion
+    def _complete(self):
+        torch = self.torch
+        torch.cuda.set_device(self._device)
+        while True:
+            with self._lock:
+                while not self._inflight:
+                    self._lock.wait()
+                rec = self._inflight[0]
+                if rec is None:
+                    return
+            kind, pend, out, ev = rec
+            if not ev.query():
+                time.sleep(0.0002)
+                # look for any finished record, not just the oldest
+                with self._lock:
+                    ready = None
+                    for r in self._inflight:
+                        if r is not None and r[3].query():
+                            ready = r
+                            break
+                    if ready is None:
+                        continue
+                    self._inflight.remove(ready)
+                    rec = ready
+            else:
+                with self._lock:
+                    self._inflight.popleft()
+            self._finish(rec)
+
+    def _finish(self, rec):
+        kind, pend, out, ev = rec
+        ev.synchronize()
+        now = time.perf_counter()
+        if kind == 'closest':
+            dist, loc, offs, counts = out
+            d, l_ = dist.cpu().numpy(), loc.cpu().numpy()
+            results = [(d[o:o + c], l_[o:o + c]) for o, c in zip(offs, counts)]
+        elif isinstance(pend[0].req, RayRequest):
+            results = [tuple(x.cpu().numpy() if hasattr(x, 'cpu') else x for x in out)]
+        else:
+            results = [out]
+        now = time.perf_counter()
+        with self._lock:
+            for p, r in zip(pend, results):
+                self._inflight_bytes -= p.bytes
+                self.latencies.append(now - p.t_submit)
+                self.completed += 1
+            self._lock.notify_all()
+        for p, r in zip(pend, results):
+            p.future.set_result(r)
