@@ -317,8 +317,96 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_rays(args):
+    """Plain-method config: 3->32x3->1 ReLU (He-normal seed 0, median-biased), camera at
+    distance 3 looking at the origin, 60 deg FOV, n_max_step 64, affine_fixed."""
+    import torch
+    niq = importlib.import_module(PKG)
+    params = niq.workloads.plain_small_model()
+    f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=True)
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    look, up, _ = niq.render.look_at(np.array([0., 0., 3.], np.float32))
+    out = {"metric": "rays/s (cast_rays, 3x32x3 ReLU MLP, affine_fixed)", "unit": "rays/s", "config": {}}
+    for res in (128, 1024):
+        roots, dirs = niq.render.generate_camera_rays(np.array([0., 0., 3.], np.float32), look, up, res=res, fov_deg=60.)
+        rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
+        res_out = {}
+        for form, persistent in (("persistent", True), ("plain", False)):
+            for _ in range(args.warmup):
+                r = niq.queries.cast_rays((f,), (params,), rt, dt, opts, persistent=persistent, return_device=True)
+            torch.cuda.synchronize()
+            times = []
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                r = niq.queries.cast_rays((f,), (params,), rt, dt, opts, persistent=persistent, return_device=True)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+            t = sum(times) / len(times)
+            steps = int(r[2].sum().item())
+            res_out[form] = {"rays_per_s": res * res / t, "ms": t * 1e3, "ray_steps_per_s": steps / t,
+                             "hits": int((r[1] > 0).sum().item())}
+        res_out["persistent_speedup"] = res_out["plain"]["ms"] / res_out["persistent"]["ms"]
+        out["config"][f"{res}x{res}"] = res_out
+    out["value"] = out["config"]["1024x1024"]["persistent"]["rays_per_s"]
+    print(json.dumps(out))
+
+
+def run_batched(args):
+    """Batched config: 512 MLPs (widths U{16..128}, depths U{2..6}, ReLU or TanH),
+    64-4096 closest-point queries each, eps 1e-3, all in one persistent launch; compared
+    with one reference-schedule call per model."""
+    import torch
+    niq = importlib.import_module(PKG)
+    n_models = args.n_models
+    t0 = time.perf_counter()
+    models = niq.workloads.batched_models(n_models)
+    qs = niq.workloads.batched_queries(n_models)
+    t_gen = time.perf_counter() - t0
+    f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(models[0], 'affine_fixed', conservative=True)
+    table = niq.batched.ModelTable(models)
+    counts = np.array([len(q) for q in qs], np.int64)
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    allq = torch.from_numpy(np.concatenate(qs)).cuda()
+    lo, hi = np.full(3, -1.2, np.float32), np.full(3, 1.2, np.float32)
+    jm = np.arange(n_models, dtype=np.int32)
+
+    def batched_step():
+        return niq.batched.closest_point_packed(f, table, jm, offs, counts, allq, lo, hi, 1e-3)
+    for _ in range(args.warmup):
+        d, l_ = batched_step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        d, l_ = batched_step()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t_b = sum(times) / len(times)
+    # one call per model, reference schedule (plain)
+    t0 = time.perf_counter()
+    n_plain = min(n_models, args.plain_models)
+    for i in range(n_plain):
+        niq.kd_tree.closest_point(f, table.models[i], lo, hi, allq[offs[i]:offs[i] + counts[i]], eps=1e-3)
+    torch.cuda.synchronize()
+    t_p = (time.perf_counter() - t0) * n_models / n_plain
+    nq = int(counts.sum())
+    print(json.dumps({"metric": "closest-point queries/s (512 MLPs in one launch)", "value": nq / t_b,
+                      "unit": "queries/s", "ms": t_b * 1e3, "queries": nq, "models": n_models,
+                      "plain_per_model_calls": {"queries_per_s": nq / t_p, "ms_extrapolated": t_p * 1e3,
+                                                "models_timed": n_plain},
+                      "batched_speedup": t_p / t_b, "model_generation_s": t_gen}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument('--config', default='tree', choices=['tree', 'rays', 'batched'])
+    ap.add_argument('--n-models', type=int, default=512)
+    ap.add_argument('--plain-models', type=int, default=64)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
@@ -329,6 +417,10 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == 'ours' else args.warmup
     if args.impl == 'reference':
         run_reference(args)
+    elif args.config == 'rays':
+        run_rays(args)
+    elif args.config == 'batched':
+        run_batched(args)
     else:
         run_ours(args)
 

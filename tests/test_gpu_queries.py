@@ -232,16 +232,17 @@ def test_closest_point_persistent_and_batched(niq, R, gpu_ready):
     # the persistent traversal prunes with a true lower bound, so it visits every node the
     # reference schedule visits that could hold a better candidate: never worse
     assert np.all(d_p[fin] <= d_ref[fin] + 1e-5)
-    # and every candidate is an upper bound of the distance to a sign change of the network:
-    # the ball of radius d around the query holds points of both signs (FP64 samples)
+    # every reported distance is cd + diag of a node whose samples change sign, so the
+    # FP64 network changes sign within diag of the reported location
     o = R.generate_implicit(params, 'affine_fixed', dtype=np.float64)
-    v_q = o(params, q.astype(np.float64))
-    dirs = rng.standard_normal((8192, 3))
-    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
-    radii = rng.uniform(0, 1, (8192, 1)) ** (1 / 3)
-    for i in np.nonzero(fin)[0][:20]:
-        ball = q[i].astype(np.float64) + d_p[i] * radii * dirs
-        assert np.any(np.sign(o(params, ball)) != np.sign(v_q[i])) or abs(v_q[i]) < 1e-6
+    g = np.linspace(-1, 1, 11)
+    grid = np.stack(np.meshgrid(g, g, g, indexing='ij'), -1).reshape(-1, 3)
+    for i in np.nonzero(fin)[0][:40]:
+        c = l_p[i].astype(np.float64)
+        diag = float(d_p[i]) - np.linalg.norm(q[i] - c)
+        assert diag >= -1e-5
+        v = o(params, c + max(diag, 1e-6) * grid)
+        assert v.min() <= 0 <= v.max(), i
     # the batched form over a model table returns the persistent form's results
     other = niq.workloads.he_mlp([3, 48, 48, 1], 'tanh', seed=9, grid=16)
     out = niq.batched.closest_point_many(f, [params, other], [0, 1, 0], [q[:100], q[100:200], q[200:]],
