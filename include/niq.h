@@ -202,11 +202,14 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
                       void* workspace, size_t workspace_bytes, void* stream);
 /* Persistent form: every query traverses its own depth-first stack on the device,
  * nearer child first; one launch.  Same candidate and pruning tests as the reference;
- * the visiting order differs, see the design doc for the resulting tolerance. */
+ * Nodes are pruned with the query-to-box distance (a true lower bound), so the result is
+ * never larger than the reference schedule's.  node_budget (<= 0: none) caps the nodes
+ * one query may visit; a query that reaches it keeps its best distance so far (still an
+ * upper bound) and the call returns NIQ_ERR_TIMEOUT after writing every result. */
 size_t niq_closest_point_persistent_workspace_size(int64_t n_queries);
 int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* opts,
                                  const float* lower, const float* upper, int64_t n_queries,
-                                 const float* query_points, float eps,
+                                 const float* query_points, float eps, int64_t node_budget,
                                  float* min_dist_out, float* min_loc_out,
                                  void* workspace, size_t workspace_bytes, void* stream);
 
@@ -223,7 +226,8 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models,
                               const int32_t* job_model, const int64_t* query_offset,
                               const int64_t* query_count, const float* query_points,
                               const float* lower, const float* upper, float eps,
-                              float* min_dist_out, float* min_loc_out, int32_t* status_out,
+                              float* min_dist_out, float* min_loc_out, int64_t node_budget,
+                              int32_t* status_out,
                               void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus

@@ -45,7 +45,7 @@ def closest_point_many(func, table, job_models, query_points_list, lower, upper,
 
 
 def closest_point_packed(func, table, job_models, offsets, counts, query_points, lower, upper, eps=0.001,
-                         status=None):
+                         status=None, node_budget=1 << 16):
     """Device-level form: all queries in one (N, 3) array (host or device), jobs as
     (model index, row offset, row count).  Returns device tensors (dist (N,), loc (N,3)).
     With ``status`` (a CUDA int32 tensor of one element) the call does not synchronise:
@@ -69,5 +69,5 @@ def closest_point_packed(func, table, job_models, offsets, counts, query_points,
         table.handles, len(table), _lib.C.byref(bo), len(jm),
         jm.ctypes.data_as(_lib.C.POINTER(_lib.C.c_int32)), jo.ctypes.data_as(_lib.C.POINTER(_lib.C.c_int64)),
         jc.ctypes.data_as(_lib.C.POINTER(_lib.C.c_int64)), _io.ptr(q), lo, hi, float(eps), _io.ptr(dist),
-        _io.ptr(loc), _io.ptr(status), _io.ptr(ws), ws_bytes, _io.stream_handle()))
+        _io.ptr(loc), int(node_budget or 0), _io.ptr(status), _io.ptr(ws), ws_bytes, _io.stream_handle()))
     return dist, loc

@@ -36,12 +36,14 @@ struct BArgs {
     unsigned long long* next_chunk;
     int* err;
     int smem_floats;             // dynamic shared memory in floats
+    long long node_budget;       // nodes one query may visit
 };
 
 // per-slot state shared by every width class (at most 64 slots per CTA)
 struct BSlots {
     float lo[64][3], hi[64][3], qp[64][3], best[64], loc[64][3], lohi[64][2];
     int top[64], act[64], qid[64], next;
+    long long nodes[64];
 };
 
 template <int TPI, bool C, bool SLOPE>
@@ -87,6 +89,7 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
             }
             s_top[item] = 1;
             s_best[item] = INFINITY;
+            S.nodes[item] = 0;
         } else {
             s_qid[item] = -1;
             s_top[item] = 0;
@@ -101,6 +104,17 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
                 a.min_dist[id] = s_best[item];
                 for (int j = 0; j < 3; ++j) a.min_loc[3 * id + j] = s_loc[item][j];
                 claim();
+            }
+            // node budget per query: past it the query keeps its best so far (an upper
+            // bound) and the call reports NIQ_ERR_TIMEOUT
+            if (s_qid[item] >= 0 && s_top[item] > 0 && ++S.nodes[item] > a.node_budget) {
+                niq_flag_error(a.err, NIQ_ERR_TIMEOUT);
+                s_top[item] = 0;
+                const long long id = s_qid[item];
+                a.min_dist[id] = s_best[item];
+                for (int j = 0; j < 3; ++j) a.min_loc[3 * id + j] = s_loc[item][j];
+                claim();
+                if (s_qid[item] >= 0) S.nodes[item] = 1;
             }
             s_act[item] = s_qid[item] >= 0;
             if (s_act[item]) {
@@ -272,7 +286,8 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
                               int32_t n_jobs, const int32_t* job_model, const int64_t* query_offset,
                               const int64_t* query_count, const float* query_points, const float* lower,
                               const float* upper, float eps, float* min_dist_out, float* min_loc_out,
-                              int32_t* status_out, void* workspace, size_t workspace_bytes, void* stream) {
+                              int64_t node_budget, int32_t* status_out, void* workspace, size_t workspace_bytes,
+                              void* stream) {
     NIQ_REQUIRE(models && opts && lower && upper && n_models >= 1 && n_jobs >= 0, NIQ_ERR_INVALID_ARG, "bad argument");
     NIQ_REQUIRE(opts->mode == NIQ_MODE_AFFINE_FIXED || opts->mode == NIQ_MODE_INTERVAL ||
                     opts->mode == NIQ_MODE_SLOPE_INTERVAL,
@@ -353,6 +368,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     a.stacks = stacks;
     a.next_chunk = next;
     a.err = status_out ? reinterpret_cast<int*>(status_out) : err;
+    a.node_budget = node_budget > 0 ? node_budget : (1ll << 62);
     const size_t smem = kSmemBudget;
     a.smem_floats = (int)(smem / 4);
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
@@ -375,7 +391,9 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     int e = 0;
     NIQ_CUDA(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
     NIQ_CUDA(cudaStreamSynchronize(s));
-    NIQ_REQUIRE(e == 0, NIQ_ERR_CAPACITY, "closest-point stack depth %d exceeded", kBStack);
+    NIQ_REQUIRE(e != NIQ_ERR_CAPACITY, NIQ_ERR_CAPACITY, "closest-point stack depth %d exceeded", kBStack);
+    NIQ_REQUIRE(e == 0, e, "closest-point node budget of %lld nodes per query exhausted; results are upper bounds",
+                (long long)a.node_budget);
     return NIQ_OK;
 }
 

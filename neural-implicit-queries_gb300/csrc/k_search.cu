@@ -93,6 +93,7 @@ struct CpArgs {
     float* min_loc;          // (Q,3)
     float eps_w;             // eps / sqrt(3)
     int interval;
+    long long node_budget;   // persistent form: nodes one query may visit
 };
 
 // ---- reference schedule: process one popped batch [pop, top) of the global stack
@@ -263,6 +264,7 @@ __global__ void __launch_bounds__(kNT) k_cp_persistent(NiqModelRef M, CpArgs a, 
     __shared__ float s_lo[ITEMS][3], s_hi[ITEMS][3], s_q[ITEMS][3], s_best[ITEMS], s_loc[ITEMS][3];
     __shared__ float s_lohi[ITEMS][2];
     __shared__ int s_top[ITEMS], s_act[ITEMS];
+    __shared__ long long s_nodes[ITEMS];
     __shared__ long long s_qid[ITEMS];
     load_header(H, M.hdr);
     __syncthreads();
@@ -280,6 +282,7 @@ __global__ void __launch_bounds__(kNT) k_cp_persistent(NiqModelRef M, CpArgs a, 
             for (int j = 0; j < 3; ++j) { s_q[item][j] = a.q[3 * k + j]; my_stack[j] = root[j]; my_stack[3 + j] = root[3 + j]; s_loc[item][j] = -777.f; }
             s_top[item] = 1;
             s_best[item] = INFINITY;
+            s_nodes[item] = 0;
         } else {
             s_qid[item] = -1;
             s_top[item] = 0;
@@ -295,6 +298,17 @@ __global__ void __launch_bounds__(kNT) k_cp_persistent(NiqModelRef M, CpArgs a, 
                 a.min_dist[id] = s_best[item];
                 for (int j = 0; j < 3; ++j) a.min_loc[3 * id + j] = s_loc[item][j];
                 claim();
+            }
+            // node budget per query: past it the traversal stops with its best so far (a
+            // valid upper bound) and the call reports NIQ_ERR_TIMEOUT
+            if (s_qid[item] >= 0 && s_top[item] > 0 && ++s_nodes[item] > a.node_budget) {
+                niq_flag_error(err, NIQ_ERR_TIMEOUT);
+                s_top[item] = 0;
+                const long long id = s_qid[item];
+                a.min_dist[id] = s_best[item];
+                for (int j = 0; j < 3; ++j) a.min_loc[3 * id + j] = s_loc[item][j];
+                claim();
+                if (s_qid[item] >= 0) s_nodes[item] = 1;
             }
             s_act[item] = s_qid[item] >= 0;
             if (s_act[item]) {
@@ -724,6 +738,7 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
     a.min_loc = min_loc_out;
     a.eps_w = eps / sqrtf(3.f);
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
+    a.node_budget = 1ll << 62;   // the reference schedule is bounded by its stack capacity
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(model->hdr.max_width);
     int rc = NIQ_OK;
@@ -768,8 +783,8 @@ size_t niq_closest_point_persistent_workspace_size(int64_t n_queries) { return c
 
 int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* opts, const float* lower,
                                  const float* upper, int64_t n_queries, const float* query_points, float eps,
-                                 float* min_dist_out, float* min_loc_out, void* workspace, size_t workspace_bytes,
-                                 void* stream) {
+                                 int64_t node_budget, float* min_dist_out, float* min_loc_out, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
     NIQ_REQUIRE(model && opts && lower && upper, NIQ_ERR_INVALID_ARG, "null argument");
     NIQ_REQUIRE(fixed_mode(opts->mode), NIQ_ERR_UNSUPPORTED, "closest_point supports interval, affine_fixed, slope_interval");
     NIQ_REQUIRE(n_queries >= 0, NIQ_ERR_INVALID_ARG, "bad sizes");
@@ -792,6 +807,7 @@ int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* o
     a.min_loc = min_loc_out;
     a.eps_w = eps / sqrtf(3.f);
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
+    a.node_budget = node_budget > 0 ? node_budget : (1ll << 62);
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(model->hdr.max_width);
     int rc = NIQ_OK;
@@ -817,7 +833,9 @@ int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* o
     int e = 0;
     NIQ_CUDA(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
     NIQ_CUDA(cudaStreamSynchronize(s));
-    NIQ_REQUIRE(e == 0, NIQ_ERR_CAPACITY, "closest-point stack depth %d exceeded", kCpStack);
+    NIQ_REQUIRE(e != NIQ_ERR_CAPACITY, NIQ_ERR_CAPACITY, "closest-point stack depth %d exceeded", kCpStack);
+    NIQ_REQUIRE(e == 0, e, "closest-point node budget of %lld nodes per query exhausted; results are upper bounds",
+                (long long)a.node_budget);
     return NIQ_OK;
 }
 

@@ -296,6 +296,56 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
 #pragma unroll
         for (int q = 0; q < NQ; ++q) qv[q] = col_of<TPI>(g, q) < L.out_pad;
 
+        // A layer with a single 4-column group (the width-1 output layer): thread g of the
+        // item sums a k-slice of all R rows x 4 columns, then the item's TPI lanes reduce
+        // with shuffles, instead of one thread looping over all k while the others idle.
+        const bool narrow = (L.out_pad == 4) && (TPI > 1) && (resident || L.in_pad * 4 + 4 <= sw_cap);
+        if (narrow) {
+            const float* A = sW + L.a_off;
+            if (!resident) {
+                __syncthreads();
+                stage_floats(sW, gW + L.a_off, L.in_pad * 4);
+                stage_floats(sW + (sw_cap - 4), gW + L.b_off, 4);
+                __syncthreads();
+                A = sW;
+            }
+            const int kg = L.in_pad >> 2;                       // k groups of 4
+            const int per = (kg + TPI - 1) / TPI;
+            const int kb = min(kg, g * per), ke = min(kg, kb + per);
+            for (int k4 = kb; k4 < ke; ++k4) {
+                const int k = 4 * k4;
+                float4 x[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) x[r] = *reinterpret_cast<const float4*>(xs + r * LD + k);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float4 av = *reinterpret_cast<const float4*>(A + (k + kk) * 4);
+                    const float a[4] = {av.x, av.y, av.z, av.w};
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
+#pragma unroll
+                        for (int c = 0; c < 4; ++c)
+                            acc[r][c] = fmaf(xv, r < R - NABS ? a[c] : fabsf(a[c]), acc[r][c]);
+                    }
+                }
+            }
+            // reduce over the item's lanes (TPI consecutive lanes of one warp)
+#pragma unroll
+            for (int off = TPI / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[r][c] += __shfl_xor_sync(0xffffffffu, acc[r][c], off);
+            // lanes g > 0 now hold copies; only g == 0 owns column group 0 below
+            if (g != 0) {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
+            }
+        }
+
         // k-chunking when the layer is staged and does not fit the buffer
         const int row_floats = L.out_pad;
         int kc = L.in_pad;
@@ -303,7 +353,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
             const int cap_rows = (sw_cap - L.out_pad) / row_floats;
             kc = min(L.in_pad, (cap_rows / 4) * 4);
         }
-        for (int k0 = 0; k0 < L.in_pad; k0 += kc) {
+        for (int k0 = 0; k0 < (narrow ? 0 : L.in_pad); k0 += kc) {
             const int k1 = min(L.in_pad, k0 + kc);
             const float* A;
             if (resident) {

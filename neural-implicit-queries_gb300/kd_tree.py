@@ -155,14 +155,20 @@ def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes
     return False, 0, 0, np.array((-777., -777., -777.), np.float32)
 
 
-def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048, persistent=False):
+NODE_BUDGET = 1 << 16   # nodes one query may visit in the persistent closest-point forms
+
+
+def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048, persistent=False,
+                  node_budget=NODE_BUDGET):
     """src/kd_tree.py:766-802: ``(min_dist (Q,), min_loc (Q, 3))``.
 
     The default runs the reference's schedule (one global LIFO stack, batch pops of
     ``batch_process_size``), which reproduces its results, order-dependent pruning
     included.  ``persistent=True`` gives every query its own depth-first traversal on
-    the device in one launch; its pruning order differs, so distances agree with the
-    reference's within about one leaf diagonal (<= eps)."""
+    the device in one launch.  It prunes with the query-to-box distance, a true lower
+    bound, so its distances are never larger than the reference schedule's.
+    ``node_budget`` caps the nodes one persistent query may visit; exhausting it raises
+    after all results (upper bounds) are written."""
     t = _io.require_cuda()
     m = device_model(params)
     bo = func.bound_opts()
@@ -176,8 +182,8 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
         ws_bytes = L.niq_closest_point_persistent_workspace_size(Q)
         ws = _io.workspace(ws_bytes)
         _lib.check(L.niq_closest_point_persistent(m.handle, _lib.C.byref(bo), _host3(lower), _host3(upper), Q,
-                                                  _io.ptr(q), float(eps), _io.ptr(dist), _io.ptr(loc), _io.ptr(ws),
-                                                  ws_bytes, _io.stream_handle()))
+                                                  _io.ptr(q), float(eps), int(node_budget or 0), _io.ptr(dist),
+                                                  _io.ptr(loc), _io.ptr(ws), ws_bytes, _io.stream_handle()))
     else:
         B = int(batch_process_size)
         cap = max(Q + 2 * B, 1 << 16)

@@ -24,7 +24,7 @@ import dataclasses
 import queue
 import threading
 import time
-from concurrent.futures import Future
+from concurrent.futures import Future, ThreadPoolExecutor
 
 import numpy as np
 
@@ -87,6 +87,10 @@ class Server:
         self.upper = np.asarray(upper, np.float32)
         self.budget = int(budget_bytes)
         self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
+        # intersections synchronise per search level: they run on their own workers/streams
+        self._isect_pool = ThreadPoolExecutor(max_workers=2)
+        self._isect_streams = [torch.cuda.Stream() for _ in range(2)]
+        self._isect_rr = 0
         self._rr = 0
         self._q = queue.Queue()
         self._inflight = collections.deque()
@@ -114,6 +118,7 @@ class Server:
         self._q.put(None)
         self._sched.join()
         self._done.join()
+        self._isect_pool.shutdown(wait=True)
 
     def stats(self):
         lat = np.array(self.latencies) * 1e3
@@ -177,40 +182,53 @@ class Server:
     def _launch(self, wave):
         torch = self.torch
         cps = [p for p in wave if isinstance(p.req, ClosestRequest)]
-        rest = [p for p in wave if not isinstance(p.req, ClosestRequest)]
+        rays = [p for p in wave if isinstance(p.req, RayRequest)]
+        isects = [p for p in wave if isinstance(p.req, IntersectRequest)]
         if cps:
+            # every closest-point request of the wave: one multi-model launch
             s = self._next_stream()
             with torch.cuda.stream(s):
                 counts = np.array([len(p.req.points) for p in cps], np.int64)
                 offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
                 pts = np.concatenate([np.asarray(p.req.points, np.float32).reshape(-1, 3) for p in cps])
-                eps = cps[0].req.eps
+                status = torch.zeros(1, dtype=torch.int32, device='cuda')
                 dist, loc = batched.closest_point_packed(self.func, self.table, [p.req.model for p in cps], offs,
-                                                         counts, pts, self.lower, self.upper, eps)
+                                                         counts, pts, self.lower, self.upper, cps[0].req.eps,
+                                                         status=status)
                 ev = torch.cuda.Event()
                 ev.record(s)
-            self._push(('closest', cps, (dist, loc, offs, counts), ev))
-        for p in rest:
+            self._push(('closest', cps, (dist, loc, offs, counts, status), ev))
+        for p in rays:
             s = self._next_stream()
             with torch.cuda.stream(s):
-                if isinstance(p.req, RayRequest):
-                    opts = p.req.opts or queries.get_default_cast_opts()
-                    m = p.req.model
-                    t, hid, cnt, _ = queries.cast_rays((self.func,), (self.params[m],),
-                                                       torch.from_numpy(np.asarray(p.req.roots, np.float32)).cuda(),
-                                                       torch.from_numpy(np.asarray(p.req.dirs, np.float32)).cuda(), opts)
-                    out = (t, hid, cnt)
-                else:
-                    pa = prepend_op(self.params[p.req.model_a], spatial_transformation())
-                    pa['0000.spatial_transformation.R'] = np.asarray(p.req.R, np.float32)
-                    pa['0000.spatial_transformation.t'] = np.asarray(p.req.t, np.float32)
-                    pb = prepend_op(self.params[p.req.model_b], spatial_transformation())
-                    found = kd_tree.find_any_intersection((self.func, self.func), (pa, pb), self.lower, self.upper,
-                                                          p.req.eps)
-                    out = found
+                opts = p.req.opts or queries.get_default_cast_opts()
+                out = queries.cast_rays((self.func,), (self.table.models[p.req.model],),
+                                        np.asarray(p.req.roots, np.float32), np.asarray(p.req.dirs, np.float32),
+                                        opts, return_device=True)
                 ev = torch.cuda.Event()
                 ev.record(s)
-            self._push(('single', [p], out, ev))
+            self._push(('rays', [p], out[:3], ev))
+        for p in isects:
+            s = self._isect_streams[self._isect_rr % len(self._isect_streams)]
+            self._isect_rr += 1
+            self._isect_pool.submit(self._run_intersection, p, s)
+
+    def _run_intersection(self, p, s):
+        torch = self.torch
+        torch.cuda.set_device(self._device)
+        with torch.cuda.stream(s):
+            pa = prepend_op(self.params[p.req.model_a], spatial_transformation())
+            pa['0000.spatial_transformation.R'] = np.asarray(p.req.R, np.float32)
+            pa['0000.spatial_transformation.t'] = np.asarray(p.req.t, np.float32)
+            pb = prepend_op(self.params[p.req.model_b], spatial_transformation())
+            out = kd_tree.find_any_intersection((self.func, self.func), (pa, pb), self.lower, self.upper, p.req.eps)
+        now = time.perf_counter()
+        with self._lock:
+            self._inflight_bytes -= p.bytes
+            self.latencies.append(now - p.t_submit)
+            self.completed += 1
+            self._lock.notify_all()
+        p.future.set_result(out)
 
     def _push(self, rec):
         with self._lock:
@@ -252,13 +270,19 @@ class Server:
         ev.synchronize()
         now = time.perf_counter()
         if kind == 'closest':
-            dist, loc, offs, counts = out
+            dist, loc, offs, counts, status = out
+            if int(status.item()) != 0:
+                err = _lib.NIQCapacityError(int(status.item()), "closest-point stack depth exceeded")
+                with self._lock:
+                    for p in pend:
+                        self._inflight_bytes -= p.bytes
+                for p in pend:
+                    p.future.set_exception(err)
+                return
             d, l_ = dist.cpu().numpy(), loc.cpu().numpy()
             results = [(d[o:o + c], l_[o:o + c]) for o, c in zip(offs, counts)]
-        elif isinstance(pend[0].req, RayRequest):
-            results = [tuple(x.cpu().numpy() if hasattr(x, 'cpu') else x for x in out)]
         else:
-            results = [out]
+            results = [tuple(x.cpu().numpy() for x in out)]
         now = time.perf_counter()
         with self._lock:
             for p, r in zip(pend, results):
