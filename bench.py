@@ -222,14 +222,9 @@ def run_ours(args):
     bf = box_flops(params)
     t_tree = sum(tree_t) / len(tree_t)
     achieved_tf = n_boxes * bf / t_tree / 1e12
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
-    except (OSError, ValueError):
-        pass
-    sm_max = float(peaks.get('sm_max_mhz', 2070.0))
+    sm_max = measured_peaks().get('sm_max_mhz', 2070.0)
     props = torch.cuda.get_device_properties(local)
-    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = fp32_peak_tflops(local)
     line = {
         "metric": "bounded boxes/s (level-set tree 256^3 + HMC, 12-sphere ReLU 3x64x4 MLP, affine_fixed)",
         "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -354,10 +349,102 @@ def run_rays(args):
     print(json.dumps(out))
 
 
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except (OSError, ValueError):
+        return {}
+
+
+def fp32_peak_tflops(device=0):
+    """FP32 FMA pipe peak: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock."""
+    import torch
+    sm_max = float(measured_peaks().get('sm_max_mhz', 2070.0))
+    return torch.cuda.get_device_properties(device).multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+
+
+def run_precision(args):
+    """Deep-model config: ReLU 3->256x8->1 (He-normal seed 7, median-biased output), rays
+    from an eye at distance 3 aimed at the origin, 60 deg FOV.  'affine_fixed' casts the
+    full 1024x1024 image.  'affine_truncate' with 256 noise terms costs about 2 x 258 x
+    256 x 256 FLOP per layer and segment, so it casts a strided 32x32 sample of the same
+    image (every 32nd ray in each direction) and classifies 4096 boxes, the kernel timed
+    per bounded box against the FP32 FMA roofline."""
+    import torch
+    niq = importlib.import_module(PKG)
+    params = niq.workloads.precision_model()
+    eye = np.array([0., 0., 3.], np.float32)
+    look, up, _ = niq.render.look_at(eye)
+    roots, dirs = niq.render.generate_camera_rays(eye, look, up, res=1024, fov_deg=60.)
+    opts = niq.queries.get_default_cast_opts()
+    layers = niq.mlp.spec_layers(params)
+    dims = [(A.shape[0], A.shape[1], act) for A, _, act in layers]
+
+    def box_flop(v, K=None):
+        """2 (rows) in out per layer: base, err and the noise rows; 'affine_truncate'
+        appends out rows after each activation and keeps K."""
+        tot, rows = 0, v
+        for i, o, act in dims:
+            tot += 2 * (rows + 2) * i * o
+            if K is not None and act != 'none':
+                rows = min(rows + o, K)
+        return tot
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            r = fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return r, sum(ts) / len(ts)
+    out = {"metric": "rays/s and bounded boxes/s, ReLU 3x256x8 MLP", "config": {"workload": "precision_relu256x8"}}
+    # full image, affine_fixed
+    f_fix, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=True)
+    rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
+    r, t = timed(lambda: niq.queries.cast_rays((f_fix,), (params,), rt, dt, opts, return_device=True),
+                 args.steps, args.warmup)
+    out["affine_fixed_1024x1024"] = {"rays_per_s": rt.shape[0] / t, "ms": t * 1e3,
+                                     "ray_steps": int(r[2].sum().item()), "hits": int((r[1] > 0).sum().item())}
+    # strided sample, affine_truncate 256
+    f_tr, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_truncate', conservative=True,
+                                                                  affine_n_truncate=256)
+    sub = (np.arange(0, 1024, 32)[:, None] * 1024 + np.arange(0, 1024, 32)[None, :]).reshape(-1)
+    rs, ds = rt[torch.from_numpy(sub).cuda()].contiguous(), dt[torch.from_numpy(sub).cuda()].contiguous()
+    r, t = timed(lambda: niq.queries.cast_rays((f_tr,), (params,), rs, ds, opts, return_device=True), 1, 1)
+    out["affine_truncate256_32x32_strided"] = {"rays_per_s": rs.shape[0] / t, "ms": t * 1e3,
+                                               "ray_steps": int(r[2].sum().item()),
+                                               "hits": int((r[1] > 0).sum().item())}
+    # box classification, both modes: 4096 axis-aligned boxes of half-width 0.01 around the surface
+    rng = np.random.default_rng(3)
+    c = torch.from_numpy(rng.uniform(-0.8, 0.8, (4096, 3)).astype(np.float32)).cuda()
+    vv = torch.from_numpy(np.tile((0.01 * np.eye(3, dtype=np.float32))[None], (4096, 1, 1))).cuda()
+    rows = {}
+    peak = fp32_peak_tflops(torch.cuda.current_device())
+    for name, f, nb, fl in (("affine_fixed", f_fix, 4096, box_flop(3)),
+                            ("affine_truncate256", f_tr, 1024, box_flop(3, 256))):
+        cc, vvv = c[:nb].contiguous(), vv[:nb].contiguous()
+        _, t = timed(lambda: f.bounds_general_box(params, cc, vvv), max(1, args.steps // 2), 1)
+        tf = nb * fl / t / 1e12
+        rows[name] = {"boxes_per_s": nb / t, "ms": t * 1e3, "boxes": nb, "flop_per_box": fl,
+                      "achieved_tflops": tf, "fp32_fma_peak_tflops": peak, "frac": tf / peak}
+    out["classify"] = rows
+    out["value"] = out["affine_fixed_1024x1024"]["rays_per_s"]
+    out["unit"] = "rays/s"
+    print(json.dumps(out))
+
+
 def run_batched(args):
     """Batched config: 512 MLPs (widths U{16..128}, depths U{2..6}, ReLU or TanH),
     64-4096 closest-point queries each, eps 1e-3, all in one persistent launch; compared
-    with one reference-schedule call per model."""
+    with one single-model persistent launch per model.  On untrained networks a query
+    may need millions of nodes, so both forms stop a query after --node-budget nodes
+    (its best candidate so far is an upper bound) and do the same work."""
     import torch
     niq = importlib.import_module(PKG)
     n_models = args.n_models
@@ -373,8 +460,11 @@ def run_batched(args):
     lo, hi = np.full(3, -1.2, np.float32), np.full(3, 1.2, np.float32)
     jm = np.arange(n_models, dtype=np.int32)
 
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+
     def batched_step():
-        return niq.batched.closest_point_packed(f, table, jm, offs, counts, allq, lo, hi, 1e-3)
+        return niq.batched.closest_point_packed(f, table, jm, offs, counts, allq, lo, hi, 1e-3, status=status,
+                                                node_budget=args.node_budget)
     for _ in range(args.warmup):
         d, l_ = batched_step()
     torch.cuda.synchronize()
@@ -387,16 +477,19 @@ def run_batched(args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
     t_b = sum(times) / len(times)
+    budget_hit = int(status.item()) == niq._lib.NIQ_ERR_TIMEOUT
     # the plain form: one single-model launch per model (same traversal, same budget)
     n_plain = min(n_models, args.plain_models)
-    for i in range(min(2, n_plain)):
+
+    def plain_call(i):
         niq.kd_tree.closest_point(f, table.models[i], lo, hi, allq[offs[i]:offs[i] + counts[i]], eps=1e-3,
-                                  persistent=True)
+                                  persistent=True, node_budget=args.node_budget, strict=False)
+    for i in range(min(2, n_plain)):
+        plain_call(i)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(n_plain):
-        niq.kd_tree.closest_point(f, table.models[i], lo, hi, allq[offs[i]:offs[i] + counts[i]], eps=1e-3,
-                                  persistent=True)
+        plain_call(i)
     torch.cuda.synchronize()
     t_p = (time.perf_counter() - t0) * n_models / n_plain
     nq = int(counts.sum())
@@ -404,14 +497,104 @@ def run_batched(args):
                       "unit": "queries/s", "ms": t_b * 1e3, "queries": nq, "models": n_models,
                       "plain_per_model_calls": {"queries_per_s": nq / t_p, "ms_extrapolated": t_p * 1e3,
                                                 "models_timed": n_plain},
-                      "batched_speedup": t_p / t_b, "model_generation_s": t_gen}))
+                      "batched_speedup": t_p / t_b, "node_budget": args.node_budget,
+                      "some_query_spent_budget": budget_hit, "model_generation_s": t_gen}))
+
+
+def make_serving_requests(niq, n, rng, max_res=512, max_points=16384):
+    """The serving mix: ray tiles (64^2..max_res^2 from a random camera at distance 3),
+    closest-point batches (1..max_points points, log-uniform, eps 1e-2, at most 1024
+    nodes per query: the models are untrained, their bounds loose) and pairwise
+    intersection tests under a random rigid transform (eps 2e-2): 45% / 45% / 10%."""
+    srv = niq.serve
+    reqs = []
+    sizes = [s for s in (64, 128, 256, 512) if s <= max_res]
+    for _ in range(n):
+        u = rng.random()
+        m = int(rng.integers(64))
+        if u < 0.45:
+            res = int(rng.choice(sizes))
+            eye = rng.standard_normal(3)
+            eye = (3.0 * eye / np.linalg.norm(eye)).astype(np.float32)
+            look, up, _ = niq.render.look_at(eye)
+            roots, dirs = niq.render.generate_camera_rays(eye, look, up, res=res, fov_deg=60.)
+            opts = niq.queries.get_default_cast_opts()
+            opts['n_max_step'] = 64
+            reqs.append(srv.RayRequest(m, roots, dirs, opts))
+        elif u < 0.9:
+            k = int(np.exp(rng.uniform(0, np.log(max_points))))
+            reqs.append(srv.ClosestRequest(m, rng.uniform(-1.2, 1.2, (k, 3)).astype(np.float32), eps=1e-2,
+                                           node_budget=1024))
+        else:
+            R = niq.workloads.random_rotation(rng)
+            reqs.append(srv.IntersectRequest(m, int(rng.integers(64)), R,
+                                             rng.uniform(-0.5, 0.5, 3).astype(np.float32), eps=2e-2))
+    return reqs
+
+
+def run_serve(args):
+    """Served config: 64 resident MLPs (width 32-256, depth 3-8, seeds 100-163), a mixed
+    request stream, 40 GB admission budget.  Measures the saturation throughput with a
+    closed batch of requests, then Poisson arrivals at fractions of it, and reports
+    p50/p99 latency per rate."""
+    import torch
+    niq = importlib.import_module(PKG)
+    models = niq.workloads.serving_models(64)
+    rng = np.random.default_rng(7)
+    srv = niq.serve.Server(models, budget_bytes=40 << 30, n_streams=4)
+    # warm up every model once (packing, uploads, kernel attributes)
+    warm = make_serving_requests(niq, 16, rng, max_res=64, max_points=64)
+    for f in [srv.submit(r) for r in warm]:
+        f.exception(timeout=600)
+    # saturation: everything submitted at once
+    sat = make_serving_requests(niq, args.serve_requests, rng, max_res=args.serve_max_res)
+    t0 = time.perf_counter()
+    futs = [srv.submit(r) for r in sat]
+    errors = sum(1 for f in futs if f.exception(timeout=1800) is not None)
+    t_sat = time.perf_counter() - t0
+    peak = len(sat) / t_sat
+    srv.latencies.clear()
+    out = {"metric": "served requests/s and p50/p99 latency (64 resident MLPs, mixed requests)",
+           "unit": "requests/s", "saturation": {"requests": len(sat), "seconds": t_sat, "req_per_s": peak,
+                                                 "errors": errors}, "rates": []}
+    for frac in args.serve_fracs:
+        rate = frac * peak
+        reqs = make_serving_requests(niq, max(8, int(rate * args.serve_seconds)), rng, max_res=args.serve_max_res)
+        srv.latencies.clear()
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        t_start = time.perf_counter()
+        t_next = t_start
+        futs = []
+        for r, gap in zip(reqs, gaps):
+            t_next += gap
+            dt = t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            futs.append(srv.submit(r))
+        errs = sum(1 for f in futs if f.exception(timeout=1800) is not None)
+        t_all = time.perf_counter() - t_start
+        st = srv.stats()
+        out["rates"].append({"fraction_of_peak": frac, "offered_req_per_s": rate, "completed": st.get("completed", 0),
+                             "achieved_req_per_s": len(reqs) / t_all, "p50_ms": st.get("p50_ms"),
+                             "p99_ms": st.get("p99_ms"), "errors": errs})
+    srv.close()
+    seventy = [r for r in out["rates"] if abs(r["fraction_of_peak"] - 0.7) < 1e-6]
+    out["value"] = peak
+    out["p99_ms_at_70pct"] = seventy[0]["p99_ms"] if seventy else None
+    print(json.dumps(out))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--config', default='tree', choices=['tree', 'rays', 'batched'])
+    ap.add_argument('--config', default='tree', choices=['tree', 'rays', 'batched', 'serve', 'precision'])
+    ap.add_argument('--serve-requests', type=int, default=200)
+    ap.add_argument('--serve-seconds', type=float, default=10.0)
+    ap.add_argument('--serve-max-res', type=int, default=512)
+    ap.add_argument('--serve-fracs', type=float, nargs='+', default=[0.3, 0.5, 0.7, 0.9])
     ap.add_argument('--n-models', type=int, default=512)
     ap.add_argument('--plain-models', type=int, default=64)
+    ap.add_argument('--node-budget', type=int, default=2048,
+                    help='closest-point nodes per query in the batched config (both forms)')
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
@@ -424,8 +607,12 @@ def main():
         run_reference(args)
     elif args.config == 'rays':
         run_rays(args)
+    elif args.config == 'precision':
+        run_precision(args)
     elif args.config == 'batched':
         run_batched(args)
+    elif args.config == 'serve':
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -63,14 +63,24 @@ extern "C" {
 
 typedef struct niq_model niq_model;
 
+/* How the growing-term modes (AFFINE_TRUNCATE, AFFINE_ALL) form their dense products:
+ * AUTO lets the library choose (FP32 FMA for now), FP32 forces FP32 FMA, 3XTF32 the tensor cores
+ * (split-precision tf32 products; needs every hidden layer activated, widths <= 256 and
+ * at most 256 noise rows).  The other modes always use FP32 FMA. */
+#define NIQ_PRODUCTS_AUTO    0
+#define NIQ_PRODUCTS_FP32    1
+#define NIQ_PRODUCTS_3XTF32  2
+
 /* Options of one range-analysis evaluation (the reference's AffineContext,
  * src/affine.py:62-76).  truncate_count is used by AFFINE_TRUNCATE, n_append by
- * AFFINE_APPEND.  conservative != 0 adds the outward rounding-error terms. */
+ * AFFINE_APPEND.  conservative != 0 adds the outward rounding-error terms.  products:
+ * NIQ_PRODUCTS_*. */
 typedef struct niq_bound_opts {
     int32_t mode;
     int32_t truncate_count;
     int32_t n_append;
     int32_t conservative;
+    int32_t products;
 } niq_bound_opts;
 
 /* The cast options dict of src/queries.py:23-36. */
@@ -120,8 +130,12 @@ int niq_classify_boxes(const niq_model* model, const niq_bound_opts* opts, int64
  * models[nfunc] are the functions of funcs_tuple; hit_id is 1-based (0 = no hit).
  * Persistent kernel: every ray steps on the device until it terminates; no host
  * round trip per iteration.  n_evals_out (device int64) counts ray-steps evaluated
- * per function.  workspace: niq_cast_rays_workspace_size() bytes. */
-size_t niq_cast_rays_workspace_size(int32_t nfunc, int64_t n);
+ * per function.  workspace: niq_cast_rays_workspace_size() bytes.
+ * The growing-term modes (TRUNCATE/APPEND/ALL) run the reference's iteration loop on
+ * the host for both entry points: per substep every live segment is bounded by the
+ * growing-term engine, then the step rule and a compaction run on the device; syncs. */
+size_t niq_cast_rays_workspace_size(const niq_model* const* models, int32_t nfunc,
+                                    const niq_bound_opts* opts, int64_t n);
 int niq_cast_rays(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
                   int64_t n, const float* roots, const float* dirs, const niq_cast_opts* cast,
                   float* t_out, int32_t* hit_id_out, int32_t* count_out, int64_t* n_evals_out,
@@ -202,8 +216,10 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
                       void* workspace, size_t workspace_bytes, void* stream);
 /* Persistent form: every query traverses its own depth-first stack on the device,
  * nearer child first; one launch.  Same candidate and pruning tests as the reference;
- * Nodes are pruned with the query-to-box distance (a true lower bound), so the result is
- * never larger than the reference schedule's.  node_budget (<= 0: none) caps the nodes
+ * Nodes are pruned when the query-to-box distance (a true lower bound) is within eps of
+ * the best candidate, so the result is never larger than the reference schedule's by more
+ * than eps (candidates already carry a leaf diagonal, <= eps, of slack).  node_budget
+ * (<= 0: none) caps the nodes
  * one query may visit; a query that reaches it keeps its best distance so far (still an
  * upper bound) and the call returns NIQ_ERR_TIMEOUT after writing every result. */
 size_t niq_closest_point_persistent_workspace_size(int64_t n_queries);

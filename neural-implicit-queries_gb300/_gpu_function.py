@@ -14,18 +14,20 @@ class GPUImplicitFunction(ImplicitFunction):
     ``mode`` is one of the range-arithmetic names of src/implicit_mlp_utils.py:12-64.
     ``conservative`` (default True) adds the outward rounding terms so that every
     returned bound contains the exact range; False reproduces the reference's
-    round-to-nearest arithmetic."""
+    round-to-nearest arithmetic.  ``products`` ('auto', 'fp32', '3xtf32') chooses how the
+    growing-term modes form their dense products (NIQ_PRODUCTS_* in include/niq.h)."""
 
-    def __init__(self, style, mode, truncate_count=-777, n_append=0, conservative=True):
+    def __init__(self, style, mode, truncate_count=-777, n_append=0, conservative=True, products='auto'):
         super().__init__(style)
         self.mode = mode
         self.truncate_count = truncate_count
         self.n_append = n_append
         self.conservative = conservative
+        self.products = products
 
     # -- options as passed to the C ABI
     def bound_opts(self):
-        return _lib.bound_opts(self.mode, self.truncate_count, self.n_append, self.conservative)
+        return _lib.bound_opts(self.mode, self.truncate_count, self.n_append, self.conservative, self.products)
 
     def device_model(self, params):
         return device_model(params)

@@ -19,6 +19,7 @@ NIQ_ERR_CAPACITY = -4
 NIQ_ERR_TIMEOUT = -5
 NIQ_ERR_UNSUPPORTED = -6
 
+PRODUCTS = {'auto': 0, 'fp32': 1, '3xtf32': 2}
 MODES = {'interval': 0, 'affine_fixed': 1, 'affine_truncate': 2, 'affine_append': 3,
          'affine_all': 4, 'slope_interval': 5}
 ACTS = {'none': 0, 'relu': 1, 'elu': 2, 'tanh': 3}
@@ -39,7 +40,7 @@ class NIQCapacityError(NIQError):
 
 class BoundOpts(C.Structure):
     _fields_ = [('mode', C.c_int32), ('truncate_count', C.c_int32), ('n_append', C.c_int32),
-                ('conservative', C.c_int32)]
+                ('conservative', C.c_int32), ('products', C.c_int32)]
 
 
 class CastOpts(C.Structure):
@@ -64,7 +65,7 @@ _SIGS = {
     'niq_eval_points': (C.c_int, [_P, _I64, _P, _P, _P]),
     'niq_classify_workspace_size': (_SZ, [_P, C.POINTER(BoundOpts), _I64, _I32]),
     'niq_classify_boxes': (C.c_int, [_P, C.POINTER(BoundOpts), _I64, _P, _P, _I32, _F32, _P, _P, _P, _SZ, _P]),
-    'niq_cast_rays_workspace_size': (_SZ, [_I32, _I64]),
+    'niq_cast_rays_workspace_size': (_SZ, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I64]),
     'niq_cast_rays': (C.c_int, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I64, _P, _P, C.POINTER(CastOpts),
                                 _P, _P, _P, _P, _P, _SZ, _P]),
     'niq_cast_rays_plain': (C.c_int, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I64, _P, _P, C.POINTER(CastOpts),
@@ -134,10 +135,12 @@ def check(rc):
     raise NIQError(rc, msg)
 
 
-def bound_opts(mode, truncate_count=-777, n_append=0, conservative=True):
+def bound_opts(mode, truncate_count=-777, n_append=0, conservative=True, products='auto'):
     if mode not in MODES:
         raise ValueError(f"invalid mode {mode!r}")
-    return BoundOpts(MODES[mode], int(truncate_count), int(n_append), 1 if conservative else 0)
+    if products not in PRODUCTS:
+        raise ValueError(f"invalid products {products!r}: one of {sorted(PRODUCTS)}")
+    return BoundOpts(MODES[mode], int(truncate_count), int(n_append), 1 if conservative else 0, PRODUCTS[products])
 
 
 def cast_opts(opts):

@@ -31,6 +31,6 @@ class AffineImplicitFunction(GPUImplicitFunction):
     """src/affine.py:17-55.  ``affine_func`` is accepted for signature compatibility and
     ignored: the spec is evaluated by the CUDA kernels."""
 
-    def __init__(self, affine_func=None, ctx=AffineContext(), conservative=True):
-        super().__init__("classify-only", ctx.mode, ctx.truncate_count, ctx.n_append, conservative)
+    def __init__(self, affine_func=None, ctx=AffineContext(), conservative=True, products='auto'):
+        super().__init__("classify-only", ctx.mode, ctx.truncate_count, ctx.n_append, conservative, products)
         self.ctx = ctx

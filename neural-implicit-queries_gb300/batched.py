@@ -45,12 +45,16 @@ def closest_point_many(func, table, job_models, query_points_list, lower, upper,
 
 
 def closest_point_packed(func, table, job_models, offsets, counts, query_points, lower, upper, eps=0.001,
-                         status=None, node_budget=1 << 16):
+                         status=None, node_budget=None):
     """Device-level form: all queries in one (N, 3) array (host or device), jobs as
     (model index, row offset, row count).  Returns device tensors (dist (N,), loc (N,3)).
+    ``node_budget`` (default kd_tree.NODE_BUDGET) caps the nodes one query may visit.
     With ``status`` (a CUDA int32 tensor of one element) the call does not synchronise:
-    the traversal status (0, or NIQ_ERR_CAPACITY) lands there."""
+    the traversal status lands there (0; NIQ_ERR_TIMEOUT when a query spent its budget,
+    its result then an upper bound; NIQ_ERR_CAPACITY when a traversal stack overflowed)."""
     t = _io.require_cuda()
+    if node_budget is None:
+        from .kd_tree import NODE_BUDGET as node_budget
     q, _ = _io.to_dev(query_points)
     q = q.reshape(-1, 3)
     n = q.shape[0]

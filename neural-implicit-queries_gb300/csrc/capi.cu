@@ -107,6 +107,7 @@ int niq_model_create(const void* packed_spec, size_t bytes, niq_model** out) {
 
 int niq_model_destroy(niq_model* model) {
     if (!model) return NIQ_OK;
+    if (model->d_tc) cudaFree(model->d_tc);
     cudaError_t e = cudaFree(model->d_blob);
     delete model;
     return e == cudaSuccess ? NIQ_OK : cuda_fail(e, "cudaFree(model)");

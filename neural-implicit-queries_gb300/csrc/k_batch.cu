@@ -37,6 +37,7 @@ struct BArgs {
     int* err;
     int smem_floats;             // dynamic shared memory in floats
     long long node_budget;       // nodes one query may visit
+    float prune_tol;             // prune when box distance >= best - prune_tol (eps)
 };
 
 // per-slot state shared by every width class (at most 64 slots per CTA)
@@ -206,7 +207,7 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
                 const float dd = fmaxf(fmaxf(__fsub_rd(lo[k], q[k]), __fsub_rd(q[k], hi[k])), 0.f);
                 bd2 = __fmaf_rd(dd, dd, bd2);
             }
-            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && __fsqrt_rd(bd2) < s_best[item]) {
+            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && __fsqrt_rd(bd2) < s_best[item] - a.prune_tol) {
                 const int t = s_top[item];
                 if (t + 2 <= kBStack) {
                     int d = 0;
@@ -369,6 +370,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     a.next_chunk = next;
     a.err = status_out ? reinterpret_cast<int*>(status_out) : err;
     a.node_budget = node_budget > 0 ? node_budget : (1ll << 62);
+    a.prune_tol = eps;
     const size_t smem = kSmemBudget;
     a.smem_floats = (int)(smem / 4);
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;

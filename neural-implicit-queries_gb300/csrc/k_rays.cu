@@ -16,7 +16,9 @@
 // k_rays<PERSISTENT=true>: CTA slots refill from a global ray counter until every ray
 // has terminated (one launch).  k_rays<PERSISTENT=false>: one reference iteration over a
 // list of live rays, appending survivors to the next list (the plain form).
+#include <vector>
 #include "niq_host.cuh"
+#include "wide_engine.cuh"
 
 namespace niq {
 
@@ -289,6 +291,183 @@ RayLayout ray_layout(long long n) {
     return L;
 }
 
+bool growing_mode(int mode) {
+    return mode == NIQ_MODE_AFFINE_TRUNCATE || mode == NIQ_MODE_AFFINE_ALL || mode == NIQ_MODE_AFFINE_APPEND;
+}
+
+// Extra workspace of the growing-term path: per live ray a segment (center, vec), two
+// hit-test points, per function a sign and two values, and the substep state; then the
+// growing-term engine's own slots (the largest over the functions).
+struct WideRayLayout {
+    size_t center, vec, pts, sign, vals, hit, hitid, can, inner, wide, total;
+};
+
+WideRayLayout wide_ray_layout(const niq_model* const* models, int nfunc, const niq_bound_opts& o, long long n,
+                              size_t base) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    WideRayLayout W;
+    W.center = base;
+    W.vec = W.center + al(12 * n);
+    W.pts = W.vec + al(12 * n);
+    W.sign = W.pts + al(24 * n);
+    W.vals = W.sign + al(4 * n * (size_t)nfunc);
+    W.hit = W.vals + al(8 * n * (size_t)nfunc);
+    W.hitid = W.hit + al(4 * n);
+    W.can = W.hitid + al(4 * n);
+    W.inner = W.can + al(4 * n);
+    W.wide = W.inner + al(4 * n);
+    size_t wmax = 0;
+    for (int f = 0; f < nfunc; ++f)
+        if (models && models[f]) {
+            const size_t b = wide_workspace_bytes(models[f]->hdr, o, 1);
+            wmax = wmax > b ? wmax : b;
+        }
+    W.total = W.wide + al(wmax) + 256;
+    return W;
+}
+
+__global__ void k_wray_prep(long long n_live, const int* live, const float* roots, const float* dirs, const float* st_t,
+                            const float* st_step, float hit_eps, float* center, float* vec, float* pts) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_live; i += (long long)gridDim.x * blockDim.x) {
+        const int id = live[i];
+        const float t = st_t[id], sz = st_step[id];
+        for (int k = 0; k < 3; ++k) {
+            const float rt = roots[3 * id + k], d = dirs[3 * id + k];
+            const float ps = __fadd_rn(rt, __fmul_rn(t, d));
+            const float hv = __fmul_rn(__fmul_rn(0.5f, sz), d);
+            center[3 * i + k] = __fadd_rn(ps, hv);
+            vec[3 * i + k] = hv;
+            pts[6 * i + k] = ps;
+            pts[6 * i + 3 + k] = __fadd_rn(rt, __fmul_rn(__fadd_rn(t, hit_eps), d));
+        }
+    }
+}
+
+// One substep for every live ray (src/queries.py:44-92) from the per-function signs and
+// point values; substep 0 also resets the outer iteration's hit state.
+__global__ void k_wray_update(long long n_live, const int* live, int nfunc, const int* sign, const float* vals,
+                              int first_substep, CastDev o, float* st_t, float* st_step, int* hit, int* hitid,
+                              int* inner) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_live; i += (long long)gridDim.x * blockDim.x) {
+        const int id = live[i];
+        if (first_substep) { hit[i] = 0; hitid[i] = 0; inner[i] = 0; }
+        const bool hit_before = hit[i] != 0;
+        bool can = !hit_before;
+        bool is_hit = hit_before;
+        int hid = hitid[i];
+        inner[i] += hit_before ? 0 : 1;
+        for (int f = 0; f < nfunc; ++f) {
+            const int bt = sign[(long long)f * n_live + i];
+            if (bt == NIQ_SIGN_UNKNOWN) can = false;
+            const float v0 = vals[(long long)f * 2 * n_live + 2 * i], v1 = vals[(long long)f * 2 * n_live + 2 * i + 1];
+            const int s0 = (v0 > 0.f) - (v0 < 0.f), s1 = (v1 > 0.f) - (v1 < 0.f);
+            if ((v0 != v0) || (v1 != v1) || s0 != s1) { hid = f + 1; is_hit = true; }
+        }
+        const float sz = st_step[id];
+        const float this_step = can ? sz : o.hit_eps;
+        if (!is_hit) st_t[id] = __fadd_rn(st_t[id], __fmul_rn(this_step, o.safety));
+        st_step[id] = fmaxf(can ? __fmul_rn(sz, o.grow) : __fmul_rn(sz, o.shrink), o.hit_eps);
+        hit[i] = is_hit;
+        hitid[i] = hid;
+    }
+}
+
+__global__ void k_wray_finish(long long n_live, const int* live, const int* hit, const int* hitid, const int* inner,
+                              CastDev o, const float* st_t, int* st_count, float* t_out, int* hit_out, int* count_out,
+                              int* live_next, unsigned long long* n_next) {
+    for (long long i0 = blockIdx.x * (long long)blockDim.x; i0 < n_live; i0 += (long long)gridDim.x * blockDim.x) {
+        const long long i = i0 + threadIdx.x;
+        bool keep = false;
+        int id = 0;
+        if (i < n_live) {
+            id = live[i];
+            const int cnt = st_count[id] + inner[i];
+            st_count[id] = cnt;
+            const float t = st_t[id];
+            const bool term = hit[i] || (t > o.max_dist) || (cnt >= o.n_max_step);
+            if (term) { t_out[id] = t; hit_out[id] = hitid[i]; count_out[id] = cnt; }
+            keep = !term;
+        }
+        const long long pos = niq_warp_append(n_next, keep);
+        if (keep) live_next[pos] = id;
+    }
+}
+
+template <bool PERSISTENT>
+int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts* opts, long long n, const float* roots,
+                const float* dirs, const niq_cast_opts* cast, float* t_out, int* hit_out, int* count_out,
+                unsigned long long* n_evals, void* workspace, size_t ws_bytes, cudaStream_t s);
+
+// The growing-term modes: a host loop over the reference's iterations, each substep
+// bounding every live segment with the growing-term engine (v = 1) and evaluating the
+// two hit-test points, then the reference's step rule and a compaction.
+int launch_rays_wide(const niq_model* const* models, int nfunc, const niq_bound_opts* opts, long long n,
+                     const float* roots, const float* dirs, const niq_cast_opts* cast, float* t_out, int* hit_out,
+                     int* count_out, unsigned long long* n_evals, void* workspace, size_t ws_bytes, cudaStream_t s) {
+    NIQ_REQUIRE(models && nfunc >= 1 && nfunc <= kMaxFuncs, NIQ_ERR_INVALID_ARG, "nfunc must be in [1, %d]", kMaxFuncs);
+    for (int f = 0; f < nfunc; ++f) NIQ_REQUIRE(models[f], NIQ_ERR_INVALID_ARG, "null model %d", f);
+    const RayLayout RL = ray_layout(n);
+    const WideRayLayout W = wide_ray_layout(models, nfunc, *opts, n, RL.total);
+    NIQ_REQUIRE(workspace && ws_bytes >= W.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", W.total);
+    NIQ_REQUIRE(n == 0 || (roots && dirs && t_out && hit_out && count_out && n_evals), NIQ_ERR_INVALID_ARG, "null array");
+    NIQ_CUDA(cudaMemsetAsync(n_evals, 0, sizeof(unsigned long long) * nfunc, s));
+    if (n == 0) return NIQ_OK;
+    char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    RayWs* ws = reinterpret_cast<RayWs*>(base + RL.hdr);
+    float* st_t = reinterpret_cast<float*>(base + RL.t);
+    float* st_step = reinterpret_cast<float*>(base + RL.step);
+    int* st_count = reinterpret_cast<int*>(base + RL.count);
+    int* live[2] = {reinterpret_cast<int*>(base + RL.live0), reinterpret_cast<int*>(base + RL.live1)};
+    float* center = reinterpret_cast<float*>(base + W.center);
+    float* vec = reinterpret_cast<float*>(base + W.vec);
+    float* pts = reinterpret_cast<float*>(base + W.pts);
+    int* sign = reinterpret_cast<int*>(base + W.sign);
+    float* vals = reinterpret_cast<float*>(base + W.vals);
+    int* hit = reinterpret_cast<int*>(base + W.hit);
+    int* hitid = reinterpret_cast<int*>(base + W.hitid);
+    int* inner = reinterpret_cast<int*>(base + W.inner);
+    void* wws = base + W.wide;
+    const size_t wws_bytes = ws_bytes - (size_t)(base - reinterpret_cast<char*>(workspace)) - W.wide;
+    const CastDev cd = to_dev(*cast);
+    NIQ_CUDA(cudaMemsetAsync(ws, 0, sizeof(RayWs), s));
+    NIQ_CUDA(cudaMemsetAsync(st_t, 0, 4 * n, s));
+    NIQ_CUDA(cudaMemsetAsync(st_count, 0, 4 * n, s));
+    fill_ray_init(st_step, live[0], n, cd.init_step, s);
+    long long n_live = n;
+    int cur = 0;
+    std::vector<unsigned long long> evals(nfunc, 0ull);
+    while (n_live > 0) {
+        const int blocks = (int)((n_live + 255) / 256 < 4096 ? (n_live + 255) / 256 : 4096);
+        for (int sub = 0; sub < cd.n_substeps; ++sub) {
+            k_wray_prep<<<blocks, 256, 0, s>>>(n_live, live[cur], roots, dirs, st_t, st_step, cd.hit_eps, center, vec, pts);
+            NIQ_CUDA(cudaGetLastError());
+            for (int f = 0; f < nfunc; ++f) {
+                int rc = wide_classify(models[f], *opts, n_live, center, vec, 1, 0.f, sign + (long long)f * n_live,
+                                       nullptr, wws, wws_bytes, s);
+                if (rc) return rc;
+                rc = niq_eval_points(models[f], 2 * n_live, pts, vals + (long long)f * 2 * n_live, s);
+                if (rc) return rc;
+                evals[f] += (unsigned long long)n_live;
+            }
+            k_wray_update<<<blocks, 256, 0, s>>>(n_live, live[cur], nfunc, sign, vals, sub == 0, cd, st_t, st_step, hit,
+                                                 hitid, inner);
+            NIQ_CUDA(cudaGetLastError());
+        }
+        NIQ_CUDA(cudaMemsetAsync(&ws->n_live_next, 0, sizeof(unsigned long long), s));
+        k_wray_finish<<<blocks, 256, 0, s>>>(n_live, live[cur], hit, hitid, inner, cd, st_t, st_count, t_out, hit_out,
+                                             count_out, live[1 - cur], &ws->n_live_next);
+        NIQ_CUDA(cudaGetLastError());
+        unsigned long long next = 0;
+        NIQ_CUDA(cudaMemcpyAsync(&next, &ws->n_live_next, sizeof(next), cudaMemcpyDeviceToHost, s));
+        NIQ_CUDA(cudaStreamSynchronize(s));
+        n_live = (long long)next;
+        cur = 1 - cur;
+    }
+    NIQ_CUDA(cudaMemcpyAsync(n_evals, evals.data(), sizeof(unsigned long long) * nfunc, cudaMemcpyHostToDevice, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    return NIQ_OK;
+}
+
 template <bool PERSISTENT>
 int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts* opts, long long n, const float* roots,
                 const float* dirs, const niq_cast_opts* cast, float* t_out, int* hit_out, int* count_out,
@@ -297,8 +476,11 @@ int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts*
     NIQ_REQUIRE(n >= 0 && n < (1ll << 31), NIQ_ERR_INVALID_ARG, "ray count %lld out of range", n);
     NIQ_REQUIRE(cast->n_substeps >= 1 && cast->hit_eps > 0.f, NIQ_ERR_INVALID_ARG, "n_substeps >= 1 and hit_eps > 0 required");
     const int mode = opts->mode;
+    if (growing_mode(mode))
+        return launch_rays_wide(models, nfunc, opts, n, roots, dirs, cast, t_out, hit_out, count_out, n_evals, workspace,
+                                ws_bytes, s);
     NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
-                NIQ_ERR_UNSUPPORTED, "cast_rays supports the interval, affine_fixed and slope_interval modes (mode %d)", mode);
+                NIQ_ERR_UNSUPPORTED, "unknown mode %d", mode);
     ModelSet S;
     int maxw, wfloats, maxlayer;
     int rc = make_set(models, nfunc, S, maxw, wfloats, maxlayer);
@@ -375,9 +557,11 @@ int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts*
 
 extern "C" {
 
-size_t niq_cast_rays_workspace_size(int32_t nfunc, int64_t n) {
-    (void)nfunc;
-    return ray_layout(n).total;
+size_t niq_cast_rays_workspace_size(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
+                                    int64_t n) {
+    const RayLayout RL = ray_layout(n);
+    if (opts && growing_mode(opts->mode)) return wide_ray_layout(models, nfunc, *opts, n, RL.total).total;
+    return RL.total;
 }
 
 int niq_cast_rays(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts, int64_t n,

@@ -94,6 +94,7 @@ struct CpArgs {
     float eps_w;             // eps / sqrt(3)
     int interval;
     long long node_budget;   // persistent form: nodes one query may visit
+    float prune_tol;         // persistent form: prune when box distance >= best - prune_tol
 };
 
 // ---- reference schedule: process one popped batch [pop, top) of the global stack
@@ -356,11 +357,13 @@ __global__ void __launch_bounds__(kNT) k_cp_persistent(NiqModelRef M, CpArgs a, 
                     for (int k = 0; k < 3; ++k) s_loc[item][k] = c[k];
                 }
             }
-            // prune with the distance from the query to the box: a true lower bound on every
+            // prune with the distance from the query to the box, a true lower bound on every
             // candidate inside it (the reference computes it, src/kd_tree.py:699, but prunes
             // with the center distance, which under depth-first order would drop subtrees
-            // that hold the closest candidate)
-            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && box_dist(q, lo, hi) < s_best[item]) {
+            // that hold the closest candidate), less a tolerance of eps: candidates carry a
+            // leaf-diagonal (<= eps) slack anyway, and proving that no node of the
+            // surface cap within eps of the best is better would visit the whole cap
+            if (type == NIQ_SIGN_UNKNOWN && !(width < a.eps_w) && box_dist(q, lo, hi) < s_best[item] - a.prune_tol) {
                 const int t = s_top[item];
                 if (t + 2 <= kCpStack) {
                     const int d = first_longest(lo, hi);
@@ -739,6 +742,7 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
     a.eps_w = eps / sqrtf(3.f);
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
     a.node_budget = 1ll << 62;   // the reference schedule is bounded by its stack capacity
+    a.prune_tol = 0.f;
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(model->hdr.max_width);
     int rc = NIQ_OK;
@@ -808,6 +812,7 @@ int niq_closest_point_persistent(const niq_model* model, const niq_bound_opts* o
     a.eps_w = eps / sqrtf(3.f);
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
     a.node_budget = node_budget > 0 ? node_budget : (1ll << 62);
+    a.prune_tol = eps;
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(model->hdr.max_width);
     int rc = NIQ_OK;

@@ -47,6 +47,8 @@ struct niq_model {
     void* d_blob;             // device: header + weights
     size_t bytes;
     int device;
+    void* d_tc = nullptr;     // device: split transposed weights for the tensor cores (built on first use)
+    long long tc_off[NIQ_MAX_LAYERS] = {};
     NiqModelRef ref() const {
         NiqModelRef r;
         r.hdr = reinterpret_cast<const NiqSpecHeader*>(d_blob);

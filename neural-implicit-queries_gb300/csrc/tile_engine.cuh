@@ -393,7 +393,10 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
             }
         }
         const float* bsrc = resident ? (sW + L.b_off) : (sW + (sw_cap - L.out_pad));
-        __syncthreads();  // all reads of the layer input done before it is overwritten
+        // All reads of the layer input are done before it is overwritten.  An item's state
+        // is read and written only by its own TPI lanes, which share one warp; the shared
+        // weight buffer has its own block barrier before every restage.
+        __syncwarp();
 
         const float gam = C ? L.gamma : 0.f;
         const float gam_next = (C && !last) ? H.layers[li + 1].gamma : 0.f;
@@ -522,11 +525,23 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                     }
                 } else {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) xs[r * LD + col] = v[r];
+                    for (int r = 0; r < R; ++r) acc[r][c] = v[r];
                 }
             }
+            // one 16-byte store per row for the thread's 4 columns (scalar stores of
+            // 4 strided columns conflicted on the shared-memory banks)
+            if (!last && qv[q]) {
+                const int col0 = col_of<TPI>(g, q);
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                    *reinterpret_cast<float4*>(xs + r * LD + col0) =
+                        make_float4(acc[r][4 * q], acc[r][4 * q + 1], acc[r][4 * q + 2], acc[r][4 * q + 3]);
+            }
         }
-        __syncthreads();  // layer output visible before the next layer reads it
+        // layer output visible before the next layer reads it (the item's own warp), and
+        // after the last layer, every item's `out` row visible to the whole block
+        if (last) __syncthreads();
+        else __syncwarp();
     }
 }
 

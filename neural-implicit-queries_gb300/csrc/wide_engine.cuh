@@ -39,7 +39,15 @@ inline long long wide_slot_floats(const NiqSpecHeader& H, const niq_bound_opts& 
 
 inline int wide_slots() { return device_info().sm_count * 2; }
 
+// The tensor-core (3xTF32) form of this engine (k_wide_tc.cu).
+bool wide_tc_eligible(const NiqSpecHeader& H, const niq_bound_opts& o, int v);
+bool wide_use_tc(const NiqSpecHeader& H, const niq_bound_opts& o, int v);
+size_t wide_tc_workspace_bytes();
+int wide_tc_classify(const niq_model* m, const niq_bound_opts& o, long long n, const float* center, const float* vecs,
+                     int v, float offset, int* sign_out, float* lohi_out, void* ws, size_t ws_bytes, cudaStream_t s);
+
 inline size_t wide_workspace_bytes(const NiqSpecHeader& H, const niq_bound_opts& o, int v) {
+    if (wide_use_tc(H, o, v)) return wide_tc_workspace_bytes();
     return (size_t)wide_slot_floats(H, o, v) * wide_slots() * 4 + 256;
 }
 
@@ -259,6 +267,13 @@ inline int wide_classify(const niq_model* m, const niq_bound_opts& o, long long 
             NIQ_REQUIRE(m->hdr.layers[i].act == NIQ_ACT_NONE || m->hdr.layers[i].out >= o.n_append, NIQ_ERR_INVALID_ARG,
                         "n_append %d exceeds layer %d width %d", o.n_append, i, m->hdr.layers[i].out);
     }
+    NIQ_REQUIRE(o.products >= NIQ_PRODUCTS_AUTO && o.products <= NIQ_PRODUCTS_3XTF32, NIQ_ERR_INVALID_ARG,
+                "unknown products %d", o.products);
+    NIQ_REQUIRE(o.products != NIQ_PRODUCTS_3XTF32 || wide_tc_eligible(m->hdr, o, v), NIQ_ERR_UNSUPPORTED,
+                "3xTF32 products need truncate_count <= 256 (or <= 256 rows in affine_all), activated hidden "
+                "layers and widths <= 256");
+    if (wide_use_tc(m->hdr, o, v))
+        return wide_tc_classify(m, o, n, center, vecs, v, offset, sign_out, lohi_out, ws, ws_bytes, s);
     const size_t need = wide_workspace_bytes(m->hdr, o, v);
     NIQ_REQUIRE(ws && ws_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed, %zu given", need, ws_bytes);
     const long long slot = wide_slot_floats(m->hdr, o, v);

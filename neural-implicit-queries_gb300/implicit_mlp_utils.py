@@ -9,8 +9,11 @@ from .slope_interval import SlopeIntervalImplicitFunction
 
 def generate_implicit_from_params(params, mode, **kwargs):
     """The mode switch of src/implicit_mlp_utils.py:23-64 for an in-memory spec.
-    Extra keyword ``conservative`` (default True) selects outward rounding."""
+    Extra keywords: ``conservative`` (default True) selects outward rounding;
+    ``products`` ('auto', 'fp32', '3xtf32') how the affine_truncate/affine_all modes form
+    their dense products."""
     cons = kwargs.get('conservative', True)
+    prod = kwargs.get('products', 'auto')
     if mode == 'sdf':
         return WeakSDFImplicitFunction(lipschitz_bound=kwargs.get('sdf_lipschitz', 1.)), params
     if mode == 'interval':
@@ -20,12 +23,12 @@ def generate_implicit_from_params(params, mode, **kwargs):
     if mode == 'affine_truncate':
         ctx = AffineContext('affine_truncate', truncate_count=kwargs['affine_n_truncate'],
                             truncate_policy=kwargs.get('affine_truncate_policy', 'absolute'))
-        return AffineImplicitFunction(None, ctx, cons), params
+        return AffineImplicitFunction(None, ctx, cons, prod), params
     if mode == 'affine_append':
         return AffineImplicitFunction(None, AffineContext('affine_append', n_append=kwargs['affine_n_append']),
                                       cons), params
     if mode == 'affine_all':
-        return AffineImplicitFunction(None, AffineContext('affine_all'), cons), params
+        return AffineImplicitFunction(None, AffineContext('affine_all'), cons, prod), params
     if mode == 'slope_interval':
         return SlopeIntervalImplicitFunction(None, cons), params
     raise RuntimeError("unrecognized mode")

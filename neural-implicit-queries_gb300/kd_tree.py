@@ -115,11 +115,13 @@ def hierarchical_marching_cubes(func, params, lower, upper, depth, n_subcell_dep
     return tris[:int(n_t.item())].cpu().numpy()
 
 
-def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes=False):
+def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes=False, max_nodes=1 << 26):
     """src/kd_tree.py:567-655: ``(found, 1, 2, loc)``, or ``(False, 0, 0, (-777,)*3)``.
     The witness ``loc`` is a sample point inside both shapes (or the midpoint of two
     negative samples in an eps-small node); which witness is returned may differ from
-    the reference's, the verdict does not.  ``viz_nodes`` is not supported."""
+    the reference's, the verdict does not.  ``viz_nodes`` is not supported.  A search
+    level may hold up to ``max_nodes`` nodes (the workspace grows up to that); beyond it
+    the call raises NIQCapacityError."""
     if viz_nodes:
         raise NotImplementedError("viz_nodes (search-tree visualisation) is a GUI feature")
     if len(func_tuple) != 2:
@@ -131,7 +133,7 @@ def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes
     ma, mb = device_model(params_tuple[0]), device_model(params_tuple[1])
     bo = fa.bound_opts()
     L = _lib.load()
-    cap = 1 << 20
+    cap = min(1 << 20, int(max_nodes))
     while True:
         ws_bytes = L.niq_intersect_workspace_size(ma.handle, mb.handle, _lib.C.byref(bo), cap)
         ws = t.empty(ws_bytes, dtype=t.uint8, device='cuda')
@@ -145,9 +147,9 @@ def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes
             break
         except _lib.NIQCapacityError:
             del ws
-            cap *= 4
-            if cap > (1 << 30):
+            if cap >= max_nodes:
                 raise
+            cap = min(cap * 4, int(max_nodes))
     f = bool(found.item())
     loc = loc.cpu().numpy()
     if f:
@@ -155,20 +157,27 @@ def find_any_intersection(func_tuple, params_tuple, lower, upper, eps, viz_nodes
     return False, 0, 0, np.array((-777., -777., -777.), np.float32)
 
 
-NODE_BUDGET = 1 << 16   # nodes one query may visit in the persistent closest-point forms
+# Nodes one query may visit in the persistent closest-point forms.  With loose bounds
+# (untrained networks) a query must refine every undecided node inside the ball of its
+# best distance down to the eps size, which can take millions of nodes; the budget keeps
+# such a query from holding the device indefinitely.
+NODE_BUDGET = 1 << 22
 
 
 def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048, persistent=False,
-                  node_budget=NODE_BUDGET):
+                  node_budget=NODE_BUDGET, strict=True):
     """src/kd_tree.py:766-802: ``(min_dist (Q,), min_loc (Q, 3))``.
 
     The default runs the reference's schedule (one global LIFO stack, batch pops of
     ``batch_process_size``), which reproduces its results, order-dependent pruning
     included.  ``persistent=True`` gives every query its own depth-first traversal on
-    the device in one launch.  It prunes with the query-to-box distance, a true lower
-    bound, so its distances are never larger than the reference schedule's.
-    ``node_budget`` caps the nodes one persistent query may visit; exhausting it raises
-    after all results (upper bounds) are written."""
+    the device in one launch.  It prunes when the query-to-box distance, a true lower
+    bound, comes within eps of the best candidate, so its distances are never larger than
+    the reference schedule's by more than eps.
+    ``node_budget`` caps the nodes one persistent query may visit.  A query that
+    exhausts it keeps its best candidate so far, a valid upper bound; the call then
+    raises NIQError (code NIQ_ERR_TIMEOUT), or with ``strict=False`` returns those
+    results."""
     t = _io.require_cuda()
     m = device_model(params)
     bo = func.bound_opts()
@@ -181,9 +190,11 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
     if persistent:
         ws_bytes = L.niq_closest_point_persistent_workspace_size(Q)
         ws = _io.workspace(ws_bytes)
-        _lib.check(L.niq_closest_point_persistent(m.handle, _lib.C.byref(bo), _host3(lower), _host3(upper), Q,
-                                                  _io.ptr(q), float(eps), int(node_budget or 0), _io.ptr(dist),
-                                                  _io.ptr(loc), _io.ptr(ws), ws_bytes, _io.stream_handle()))
+        rc = L.niq_closest_point_persistent(m.handle, _lib.C.byref(bo), _host3(lower), _host3(upper), Q,
+                                            _io.ptr(q), float(eps), int(node_budget or 0), _io.ptr(dist),
+                                            _io.ptr(loc), _io.ptr(ws), ws_bytes, _io.stream_handle())
+        if strict or rc != _lib.NIQ_ERR_TIMEOUT:
+            _lib.check(rc)
     else:
         B = int(batch_process_size)
         cap = max(Q + 2 * B, 1 << 16)

@@ -56,9 +56,9 @@ def cast_rays(funcs_tuple, params_tuple, roots, dirs, opts, persistent=True, ret
     cnt = t.empty(n, dtype=t.int32, device='cuda')
     nev = t.zeros(len(models), dtype=t.int64, device='cuda')
     L = _lib.load()
-    ws_bytes = L.niq_cast_rays_workspace_size(len(models), n)
-    ws = _io.workspace(ws_bytes)
     handles = (_lib.C.c_void_p * len(models))(*[m.handle.value for m in models])
+    ws_bytes = L.niq_cast_rays_workspace_size(handles, len(models), _lib.C.byref(bo), n)
+    ws = _io.workspace(ws_bytes)
     co = _lib.cast_opts(opts)
     fn = L.niq_cast_rays if persistent else L.niq_cast_rays_plain
     _lib.check(fn(handles, len(models), _lib.C.byref(bo), n, _io.ptr(rt), _io.ptr(dt), _lib.C.byref(co),

@@ -46,6 +46,7 @@ class ClosestRequest:
     model: int
     points: np.ndarray
     eps: float = 1e-3
+    node_budget: int = 1 << 16   # nodes per query; past it the result is an upper bound
 
 
 @dataclasses.dataclass
@@ -86,6 +87,7 @@ class Server:
         self.lower = np.asarray(lower, np.float32)
         self.upper = np.asarray(upper, np.float32)
         self.budget = int(budget_bytes)
+        self.intersect_max_nodes = 1 << 20   # per search level; larger searches fail fast
         self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
         # intersections synchronise per search level: they run on their own workers/streams
         self._isect_pool = ThreadPoolExecutor(max_workers=2)
@@ -99,6 +101,7 @@ class Server:
         self._stop = False
         self.latencies = []
         self.completed = 0
+        self.budget_exhausted = 0   # closest-point launches in which a query spent its node budget
         self._sched = threading.Thread(target=self._schedule, daemon=True)
         self._done = threading.Thread(target=self._complete, daemon=True)
         self._device = torch.cuda.current_device()
@@ -125,7 +128,8 @@ class Server:
         if lat.size == 0:
             return {"completed": 0}
         return {"completed": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean())}
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "closest_budget_exhausted": self.budget_exhausted}
 
     # ------------------------------------------------------------------ scheduler
     def _next_stream(self):
@@ -184,20 +188,23 @@ class Server:
         cps = [p for p in wave if isinstance(p.req, ClosestRequest)]
         rays = [p for p in wave if isinstance(p.req, RayRequest)]
         isects = [p for p in wave if isinstance(p.req, IntersectRequest)]
-        if cps:
-            # every closest-point request of the wave: one multi-model launch
+        groups = collections.defaultdict(list)
+        for p in cps:
+            groups[(float(p.req.eps), int(p.req.node_budget))].append(p)
+        for (eps, budget), grp in groups.items():
+            # the wave's closest-point requests with one (eps, budget): one multi-model launch
             s = self._next_stream()
             with torch.cuda.stream(s):
-                counts = np.array([len(p.req.points) for p in cps], np.int64)
+                counts = np.array([len(p.req.points) for p in grp], np.int64)
                 offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
-                pts = np.concatenate([np.asarray(p.req.points, np.float32).reshape(-1, 3) for p in cps])
+                pts = np.concatenate([np.asarray(p.req.points, np.float32).reshape(-1, 3) for p in grp])
                 status = torch.zeros(1, dtype=torch.int32, device='cuda')
-                dist, loc = batched.closest_point_packed(self.func, self.table, [p.req.model for p in cps], offs,
-                                                         counts, pts, self.lower, self.upper, cps[0].req.eps,
-                                                         status=status)
+                dist, loc = batched.closest_point_packed(self.func, self.table, [p.req.model for p in grp], offs,
+                                                         counts, pts, self.lower, self.upper, eps,
+                                                         status=status, node_budget=budget)
                 ev = torch.cuda.Event()
                 ev.record(s)
-            self._push(('closest', cps, (dist, loc, offs, counts, status), ev))
+            self._push(('closest', grp, (dist, loc, offs, counts, status), ev))
         for p in rays:
             s = self._next_stream()
             with torch.cuda.stream(s):
@@ -216,19 +223,27 @@ class Server:
     def _run_intersection(self, p, s):
         torch = self.torch
         torch.cuda.set_device(self._device)
-        with torch.cuda.stream(s):
-            pa = prepend_op(self.params[p.req.model_a], spatial_transformation())
-            pa['0000.spatial_transformation.R'] = np.asarray(p.req.R, np.float32)
-            pa['0000.spatial_transformation.t'] = np.asarray(p.req.t, np.float32)
-            pb = prepend_op(self.params[p.req.model_b], spatial_transformation())
-            out = kd_tree.find_any_intersection((self.func, self.func), (pa, pb), self.lower, self.upper, p.req.eps)
+        out, exc = None, None
+        try:
+            with torch.cuda.stream(s):
+                pa = prepend_op(self.params[p.req.model_a], spatial_transformation())
+                pa['0000.spatial_transformation.R'] = np.asarray(p.req.R, np.float32)
+                pa['0000.spatial_transformation.t'] = np.asarray(p.req.t, np.float32)
+                pb = prepend_op(self.params[p.req.model_b], spatial_transformation())
+                out = kd_tree.find_any_intersection((self.func, self.func), (pa, pb), self.lower, self.upper,
+                                                    p.req.eps, max_nodes=self.intersect_max_nodes)
+        except Exception as e:   # capacity or budget exhausted: the request fails, the server goes on
+            exc = e
         now = time.perf_counter()
         with self._lock:
             self._inflight_bytes -= p.bytes
             self.latencies.append(now - p.t_submit)
             self.completed += 1
             self._lock.notify_all()
-        p.future.set_result(out)
+        if exc is not None:
+            p.future.set_exception(exc)
+        else:
+            p.future.set_result(out)
 
     def _push(self, rec):
         with self._lock:
@@ -271,8 +286,17 @@ class Server:
         now = time.perf_counter()
         if kind == 'closest':
             dist, loc, offs, counts, status = out
-            if int(status.item()) != 0:
-                err = _lib.NIQCapacityError(int(status.item()), "closest-point stack depth exceeded")
+            code = int(status.item())
+            if code == _lib.NIQ_ERR_TIMEOUT:
+                # some query spent its node budget: its distance is an upper bound; the
+                # results are still delivered and the event is counted
+                with self._lock:
+                    self.budget_exhausted += 1
+            elif code != 0:
+                if code == _lib.NIQ_ERR_CAPACITY:
+                    err = _lib.NIQCapacityError(code, "closest-point stack depth exceeded")
+                else:
+                    err = _lib.NIQError(code, "closest-point traversal failed")
                 with self._lock:
                     for p in pend:
                         self._inflight_bytes -= p.bytes

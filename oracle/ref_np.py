@@ -306,6 +306,56 @@ def affine_bounds(params, ctx, center, vecs, dtype=np.float32):
     return may_contain_bounds(base, aff, err)
 
 
+def conservative_affine_bounds_model(params, mode, center, vecs, gammas):
+    """FP64 model of the CUDA kernels' outward-rounding scheme for 'interval' and
+    'affine_fixed' with ReLU layers: the reference's rules plus, per dense layer with
+    rounding factor ``gammas[l]``, the fold gamma(|base| + sum|aff|) into the err input,
+    the (1 + 2 gamma) scale and gamma|b| on the err output, and 2^-23 (|base'| + alpha S)
+    for the linearisation's rounding.  It isolates the cost of those terms from FP32
+    arithmetic: the kernels' widths must agree with it up to FP32 noise."""
+    center = np.asarray(center, np.float64)
+    vecs = np.asarray(vecs, np.float64)
+    layers = [op for op in spec_ops(params, np.float64)]
+    dense = [(op[1], op[2] if op[2] is not None else np.zeros(op[1].shape[1])) for op in layers if op[0] == 'dense']
+    acts = []
+    for op in layers:
+        if op[0] == 'dense':
+            acts.append('none')
+        elif op[0] in ('relu', 'elu', 'tanh'):
+            acts[-1] = op[0]
+    base = center
+    if mode == 'interval':
+        aff = np.zeros((center.shape[0], 0, 3))
+        err = np.sum(np.abs(vecs), axis=1)
+    else:
+        aff = vecs
+        err = np.zeros_like(center)
+    err = err + gammas[0] * (np.abs(base) + np.abs(aff).sum(1))
+    for li, ((A, b), act) in enumerate(zip(dense, acts)):
+        g = gammas[li]
+        base, aff, err = base @ A + b, aff @ A, (err @ np.abs(A)) * (1 + 2 * g) + g * np.abs(b)
+        if act == 'relu':
+            S = np.abs(aff).sum(1)
+            lo, hi = base - (S + err), base + (S + err)
+            w = np.where(hi - lo == 0, 1., hi - lo)
+            a = np.where(lo >= 0, 1., np.where(hi < 0, 0., (np.maximum(hi, 0) - np.maximum(lo, 0)) / w))
+            a = np.clip(np.nan_to_num(a), 0, 1)
+            rhi = np.where((lo >= 0) | (hi < 0), 0., np.maximum(np.maximum(-a * lo, hi - a * hi), 0))
+            nb = a * base + rhi / 2
+            aff = a[:, None, :] * aff
+            err = a * err + rhi / 2 + 2 ** -23 * (np.abs(nb) + a * S)
+            base = nb
+            if li + 1 < len(dense):
+                err = err + gammas[li + 1] * (np.abs(base) + a * S)
+        elif act != 'none':
+            raise ValueError("the model covers ReLU networks only")
+        elif li + 1 < len(dense):
+            err = err + gammas[li + 1] * (np.abs(base) + np.abs(aff).sum(1))
+    base, aff, err = base[:, 0], aff[:, :, 0], err[:, 0]
+    rad = np.abs(aff).sum(1) + err
+    return base - rad, base + rad
+
+
 def sign_from_bounds(lower, upper, offset=0.):
     """src/affine.py:50-53 and src/slope_interval.py:44-47."""
     out = np.full(lower.shape, SIGN_UNKNOWN, dtype=np.int32)

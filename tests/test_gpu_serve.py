@@ -14,7 +14,9 @@ def test_serve_mix_equals_alone(niq, gpu_ready):
     rng = np.random.default_rng(0)
     reqs = []
     for i in range(12):
-        reqs.append(niq.serve.ClosestRequest(int(rng.integers(6)), rng.uniform(-1.2, 1.2, (int(rng.integers(1, 300)), 3)).astype(np.float32)))
+        reqs.append(niq.serve.ClosestRequest(int(rng.integers(6)),
+                                             rng.uniform(-1.2, 1.2, (int(rng.integers(1, 300)), 3)).astype(np.float32),
+                                             eps=1e-2))
     for i in range(5):
         eye = rng.standard_normal(3)
         eye = (3.0 * eye / np.linalg.norm(eye)).astype(np.float32)
@@ -36,7 +38,7 @@ def test_serve_mix_equals_alone(niq, gpu_ready):
     for k, r in enumerate(reqs):
         if isinstance(r, niq.serve.ClosestRequest):
             d, l_ = niq.kd_tree.closest_point(f, models[r.model], srv.lower, srv.upper, r.points, eps=r.eps,
-                                              persistent=True)
+                                              persistent=True, node_budget=r.node_budget, strict=False)
             np.testing.assert_array_equal(got[k][0], d)
             np.testing.assert_array_equal(got[k][1], l_)
         elif isinstance(r, niq.serve.RayRequest):
