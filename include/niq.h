@@ -64,7 +64,8 @@ extern "C" {
 typedef struct niq_model niq_model;
 
 /* How the growing-term modes (AFFINE_TRUNCATE, AFFINE_ALL) form their dense products:
- * AUTO lets the library choose (FP32 FMA for now), FP32 forces FP32 FMA, 3XTF32 the tensor cores
+ * AUTO picks the tensor cores where the noise rows x layer width are dense (hidden
+ * widths >= 128 and >= 64 rows), FP32 forces FP32 FMA, 3XTF32 forces the tensor cores
  * (split-precision tf32 products; needs every hidden layer activated, widths <= 256 and
  * at most 256 noise rows).  The other modes always use FP32 FMA. */
 #define NIQ_PRODUCTS_AUTO    0
@@ -171,6 +172,34 @@ int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts,
                             int64_t node_terminate_thresh, float offset, int32_t flags,
                             int64_t node_capacity, int64_t* counts_out,
                             void* workspace, size_t workspace_bytes, void* stream);
+/* The level-set tree for callers that cannot allocate device memory when they call:
+ * hosts whose device memory comes from a fixed pool or arena they cannot grow (the
+ * allocator would fail or fragment it), plug-ins that are handed only pre-allocated
+ * buffers, and latency-critical loops that must not enter the allocator (a device
+ * allocation can synchronise the whole device).  No counterpart in the reference (it
+ * has no allocation-free path).
+ * - No device memory is allocated, by this call or by a model handle: the caller passes
+ *   the packed spec twice, a host copy (validated and used for launch planning) and a
+ *   16-byte-aligned device copy that the kernels read.
+ * - Scratch (level counters and two level buffers) is a static device array of the
+ *   library, NIQ_STATIC_TREE_NODES nodes per level (about 3 MB), which every GPU that
+ *   loads the library holds until the process exits.  A level, or a result list, larger
+ *   than NIQ_STATIC_TREE_NODES nodes fails with NIQ_ERR_CAPACITY.
+ * - Results go to the caller's arrays, each (NIQ_STATIC_TREE_NODES, 3) float32 (interior
+ *   and exterior only when requested in flags); counts_out as for niq_levelset_tree.
+ * - The first call on a device looks up the scratch array's device address; make that
+ *   first call before any stream capture.  Every call clears the counters it needs.
+ * - All calls share the one scratch array: calls that overlap on the GPU (two streams,
+ *   or two host threads) race and corrupt each other's results.  Syncs the stream. */
+#define NIQ_STATIC_TREE_NODES 65536
+int niq_levelset_tree_static(const void* packed_spec_host, const void* packed_spec_device,
+                             size_t spec_bytes, const niq_bound_opts* opts,
+                             const float* lower, const float* upper, int32_t split_depth,
+                             int64_t node_terminate_thresh, float offset, int32_t flags,
+                             float* unknown_lower, float* unknown_upper,
+                             float* interior_lower, float* interior_upper,
+                             float* exterior_lower, float* exterior_upper,
+                             int64_t* counts_out, void* stream);
 /* Device pointers into a finished tree workspace: kind 0 unknown, 1 interior,
  * 2 exterior; lower/upper are (node_capacity, 3) arrays whose first count rows hold
  * the result. */

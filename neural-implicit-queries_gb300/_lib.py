@@ -75,6 +75,8 @@ _SIGS = {
     'niq_levelset_tree_plain': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
                                           _SZ, _P]),
     'niq_tree_result': (C.c_int, [_P, _I64, _I32, _I32, C.POINTER(_P), C.POINTER(_P)]),
+    'niq_levelset_tree_static': (C.c_int, [_P, _P, _SZ, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32,
+                                           _P, _P, _P, _P, _P, _P, _P, _P]),
     'niq_hmc_workspace_size': (_SZ, []),
     'niq_hmc_extract': (C.c_int, [_P, _I64, _P, _P, _I32, _P, _I64, _P, _P, _SZ, _P]),
     'niq_mc_table': (C.c_int, [C.POINTER(_I32)]),

@@ -40,7 +40,7 @@ const DeviceInfo& device_info() {
 
 // Validates a packed spec.  Mirrors the checks the reference performs while walking
 // the dict (src/mlp.py:117-144): every op resolvable, shapes chained.
-static int validate_spec(const NiqSpecHeader& H, size_t bytes) {
+int validate_spec(const NiqSpecHeader& H, size_t bytes) {
     NIQ_REQUIRE(H.magic == NIQ_SPEC_MAGIC, NIQ_ERR_BAD_SPEC, "bad spec magic 0x%08x", H.magic);
     NIQ_REQUIRE(H.n_layers >= 1 && H.n_layers <= NIQ_MAX_LAYERS, NIQ_ERR_BAD_SPEC, "bad layer count %d", H.n_layers);
     NIQ_REQUIRE(H.in_dim == 3, NIQ_ERR_BAD_SPEC, "input dimension must be 3, got %d", H.in_dim);

@@ -13,6 +13,7 @@
 // levels.  k_tree<COOP=false>: one level per launch, the host reads the next level's
 // size after each (the plain form, as the reference's per-level host loop).
 // Node order inside a level is whatever the atomics produce; results are node sets.
+#include <mutex>
 #include "niq_host.cuh"
 
 namespace niq {
@@ -339,3 +340,150 @@ int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32
 }
 
 }  // extern "C"
+
+// ==========================================================================================
+// Level-set tree without device allocation.
+//
+// For callers that cannot allocate device memory at the time of the call: hosts whose
+// device memory is owned by a pool or arena they cannot grow, plug-ins handed only
+// pre-allocated buffers, and latency-critical loops that must not enter the allocator
+// (a device allocation can synchronise the device).  The tree's scratch (level counters and two
+// ping-pong node buffers) lives in the file-scope array below, which every GPU that
+// loads the library holds until the process exits; the model blob, the root box and the
+// result arrays come from the caller.
+// ==========================================================================================
+namespace niq {
+
+// Largest number of nodes one level may hold (each node is 24 bytes).
+constexpr long long kStaticTreeNodes = NIQ_STATIC_TREE_NODES;
+constexpr size_t kStaticTreeHdr = (sizeof(TreeWs) + 255) & ~size_t(255);
+constexpr size_t kStaticTreeBytes = kStaticTreeHdr + 2 * (size_t)kStaticTreeNodes * 24;
+
+static __device__ __align__(256) unsigned char g_static_tree_scratch[kStaticTreeBytes];
+
+static void* g_static_tree_ptr[64] = {nullptr};
+static std::mutex g_static_tree_mu;
+
+// Device address of the scratch array on the current device, looked up once per device.
+static int static_tree_scratch(void** out) {
+    int dev = 0;
+    NIQ_CUDA(cudaGetDevice(&dev));
+    NIQ_REQUIRE(dev >= 0 && dev < 64, NIQ_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_static_tree_mu);
+    if (!g_static_tree_ptr[dev]) {
+        void* p = nullptr;
+        NIQ_CUDA(cudaGetSymbolAddress(&p, g_static_tree_scratch));
+        g_static_tree_ptr[dev] = p;
+    }
+    *out = g_static_tree_ptr[dev];
+    return NIQ_OK;
+}
+
+// Clears the counters of the scratch header and writes the root node (no host copies).
+__global__ void k_tree_static_init(TreeWs* ws, float* lo0, float* hi0, float l0, float l1, float l2, float u0,
+                                   float u1, float u2) {
+    unsigned int* w = reinterpret_cast<unsigned int*>(ws);
+    for (size_t i = threadIdx.x; i < sizeof(TreeWs) / 4; i += blockDim.x) w[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        lo0[0] = l0; lo0[1] = l1; lo0[2] = l2;
+        hi0[0] = u0; hi0[1] = u1; hi0[2] = u2;
+        ws->level_count[0] = 1ull;
+    }
+}
+
+}  // namespace niq
+
+extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void* packed_spec_device,
+                                        size_t spec_bytes, const niq_bound_opts* opts, const float* lower,
+                                        const float* upper, int32_t split_depth, int64_t node_terminate_thresh,
+                                        float offset, int32_t flags, float* unknown_lower, float* unknown_upper,
+                                        float* interior_lower, float* interior_upper, float* exterior_lower,
+                                        float* exterior_upper, int64_t* counts_out, void* stream) {
+    using namespace niq;
+    NIQ_REQUIRE(packed_spec_host && packed_spec_device && opts && lower && upper && counts_out && unknown_lower &&
+                    unknown_upper,
+                NIQ_ERR_INVALID_ARG, "null argument");
+    NIQ_REQUIRE(spec_bytes >= sizeof(NiqSpecHeader), NIQ_ERR_BAD_SPEC, "spec too short (%zu bytes)", spec_bytes);
+    NIQ_REQUIRE(reinterpret_cast<uintptr_t>(packed_spec_device) % 16 == 0, NIQ_ERR_INVALID_ARG,
+                "the device copy of the spec must be 16-byte aligned");
+    NiqSpecHeader H;
+    memcpy(&H, packed_spec_host, sizeof(H));
+    int rc = validate_spec(H, spec_bytes);
+    if (rc) return rc;
+    const int mode = opts->mode;
+    NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
+                NIQ_ERR_UNSUPPORTED, "the tree kernels support the interval, affine_fixed and slope_interval modes");
+    NIQ_REQUIRE(split_depth >= 0 || node_terminate_thresh > 0, NIQ_ERR_INVALID_ARG,
+                "must specify at least one of node_terminate_thresh or split_depth as a terminating condition");
+    NIQ_REQUIRE(split_depth < kTreeMaxLevels, NIQ_ERR_INVALID_ARG, "split_depth %d exceeds %d", split_depth,
+                kTreeMaxLevels - 1);
+    NIQ_REQUIRE(!(flags & NIQ_TREE_WITH_INTERIOR) || (interior_lower && interior_upper), NIQ_ERR_INVALID_ARG,
+                "interior output arrays required by the flags");
+    NIQ_REQUIRE(!(flags & NIQ_TREE_WITH_EXTERIOR) || (exterior_lower && exterior_upper), NIQ_ERR_INVALID_ARG,
+                "exterior output arrays required by the flags");
+    void* scratch = nullptr;
+    rc = static_tree_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    char* base = reinterpret_cast<char*>(scratch);
+    TreeWs* ws = reinterpret_cast<TreeWs*>(base);
+    TreeBufs B;
+    const long long cap = kStaticTreeNodes;
+    for (int i = 0; i < 2; ++i) {
+        B.lvl_lo[i] = reinterpret_cast<float*>(base + kStaticTreeHdr + (size_t)i * cap * 24);
+        B.lvl_hi[i] = B.lvl_lo[i] + 3 * cap;
+    }
+    B.res_lo[0] = unknown_lower;  B.res_hi[0] = unknown_upper;
+    B.res_lo[1] = interior_lower; B.res_hi[1] = interior_upper;
+    B.res_lo[2] = exterior_lower; B.res_hi[2] = exterior_upper;
+    B.cap = cap;
+    k_tree_static_init<<<1, 256, 0, s>>>(ws, B.lvl_lo[0], B.lvl_hi[0], lower[0], lower[1], lower[2], upper[0],
+                                          upper[1], upper[2]);
+    NIQ_CUDA(cudaGetLastError());
+    TreeParams P;
+    P.n_rounds = split_depth >= 0 ? split_depth + 1 : kTreeMaxLevels;
+    P.thresh = node_terminate_thresh > 0 ? node_terminate_thresh : (1ll << 62);
+    P.offset = offset;
+    P.with_interior = (flags & NIQ_TREE_WITH_INTERIOR) != 0;
+    P.with_exterior = (flags & NIQ_TREE_WITH_EXTERIOR) != 0;
+    P.mode_interval = mode == NIQ_MODE_INTERVAL;
+    NiqModelRef M;
+    M.hdr = reinterpret_cast<const NiqSpecHeader*>(packed_spec_device);
+    M.w = reinterpret_cast<const float*>(reinterpret_cast<const char*>(packed_spec_device) + sizeof(NiqSpecHeader));
+    const bool cons = opts->conservative != 0, slope = mode == NIQ_MODE_SLOPE_INTERVAL;
+    const int tpi = tpi_for_width(H.max_width);
+    auto run = [&](auto kern, int R, int TPIv) -> int {
+        const int items = kNT / TPIv;
+        const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
+        SmemPlan p = plan_smem(state, H.n_weight_floats, max_layer_floats(H));
+        NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * H.max_width, NIQ_ERR_UNSUPPORTED, "shared memory too small");
+        int r2 = prepare_kernel(kern, p.bytes);
+        if (r2) return r2;
+        int per_sm = 0;
+        NIQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kNT, p.bytes));
+        NIQ_REQUIRE(per_sm >= 1, NIQ_ERR_UNSUPPORTED, "tree kernel does not fit on an SM");
+        const int grid = per_sm * device_info().sm_count;
+        int level0 = 0;
+        int fixed = p.fixed_floats, swc = p.sw_cap, res = p.resident;
+        void* args[] = {&M, &P, &ws, &B, &level0, &fixed, &swc, &res};
+        NIQ_CUDA(cudaLaunchCooperativeKernel((const void*)kern, grid, kNT, args, p.bytes, s));
+        return NIQ_OK;
+    };
+#define NIQ_TREE_S(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_tree<TPI, CC, SL, true>, SL ? 8 : 5, TPI); })
+    if (slope) { if (cons) { NIQ_TREE_S(true, true); } else { NIQ_TREE_S(false, true); } }
+    else { if (cons) { NIQ_TREE_S(true, false); } else { NIQ_TREE_S(false, false); } }
+#undef NIQ_TREE_S
+    if (rc) return rc;
+    k_tree_finish<<<1, 1, 0, s>>>(ws, reinterpret_cast<long long*>(counts_out));
+    NIQ_CUDA(cudaGetLastError());
+    int err = 0;
+    NIQ_CUDA(cudaMemcpyAsync(&err, &ws->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    NIQ_REQUIRE(err == 0, err,
+                err == NIQ_ERR_CAPACITY
+                    ? "a level or a result list outgrew the static scratch of %lld nodes (NIQ_STATIC_TREE_NODES)"
+                    : "tree kernel error (%lld)",
+                err == NIQ_ERR_CAPACITY ? cap : (long long)err);
+    return NIQ_OK;
+}

@@ -10,6 +10,8 @@
 namespace niq {
 
 void set_error(const char* fmt, ...);
+// Checks a packed spec header against its byte size (capi.cu).
+int validate_spec(const NiqSpecHeader& H, size_t bytes);
 int cuda_fail(cudaError_t e, const char* where);
 
 #define NIQ_CUDA(call)                                                 \
