@@ -365,11 +365,12 @@ def fp32_peak_tflops(device=0):
 
 def run_precision(args):
     """Deep-model config: ReLU 3->256x8->1 (He-normal seed 7, median-biased output), rays
-    from an eye at distance 3 aimed at the origin, 60 deg FOV.  'affine_fixed' casts the
-    full 1024x1024 image.  'affine_truncate' with 256 noise terms costs about 2 x 258 x
-    256 x 256 FLOP per layer and segment, so it casts a strided 32x32 sample of the same
-    image (every 32nd ray in each direction) and classifies 4096 boxes, the kernel timed
-    per bounded box against the FP32 FMA roofline."""
+    from an eye at distance 3 aimed at the origin, 60 deg FOV, the reference's default
+    cast options.  'affine_truncate' with 256 noise terms costs about 2 x 258 x 256 x 256
+    FLOP per layer and segment, so the casts use a strided 32x32 sample of the 1024x1024
+    image (every 32nd ray in each direction); 1024 boxes of half-width 0.01 are classified
+    per form.  Forms: 'affine_fixed' (FP32 FMA tile engine) and 'affine_truncate' 256
+    with FP32 FMA products or 3xTF32 tensor-core products."""
     import torch
     niq = importlib.import_module(PKG)
     params = niq.workloads.precision_model()
@@ -403,39 +404,42 @@ def run_precision(args):
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1) / 1e3)
         return r, sum(ts) / len(ts)
-    out = {"metric": "rays/s and bounded boxes/s, ReLU 3x256x8 MLP", "config": {"workload": "precision_relu256x8"}}
-    # full image, affine_fixed
-    f_fix, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=True)
-    rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
-    r, t = timed(lambda: niq.queries.cast_rays((f_fix,), (params,), rt, dt, opts, return_device=True),
-                 args.steps, args.warmup)
-    out["affine_fixed_1024x1024"] = {"rays_per_s": rt.shape[0] / t, "ms": t * 1e3,
-                                     "ray_steps": int(r[2].sum().item()), "hits": int((r[1] > 0).sum().item())}
-    # strided sample, affine_truncate 256
-    f_tr, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_truncate', conservative=True,
-                                                                  affine_n_truncate=256)
     sub = (np.arange(0, 1024, 32)[:, None] * 1024 + np.arange(0, 1024, 32)[None, :]).reshape(-1)
-    rs, ds = rt[torch.from_numpy(sub).cuda()].contiguous(), dt[torch.from_numpy(sub).cuda()].contiguous()
-    r, t = timed(lambda: niq.queries.cast_rays((f_tr,), (params,), rs, ds, opts, return_device=True), 1, 1)
-    out["affine_truncate256_32x32_strided"] = {"rays_per_s": rs.shape[0] / t, "ms": t * 1e3,
-                                               "ray_steps": int(r[2].sum().item()),
-                                               "hits": int((r[1] > 0).sum().item())}
-    # box classification, both modes: 4096 axis-aligned boxes of half-width 0.01 around the surface
+    rs = torch.from_numpy(roots[sub]).cuda()
+    ds = torch.from_numpy(dirs[sub]).cuda()
     rng = np.random.default_rng(3)
-    c = torch.from_numpy(rng.uniform(-0.8, 0.8, (4096, 3)).astype(np.float32)).cuda()
-    vv = torch.from_numpy(np.tile((0.01 * np.eye(3, dtype=np.float32))[None], (4096, 1, 1))).cuda()
-    rows = {}
-    peak = fp32_peak_tflops(torch.cuda.current_device())
-    for name, f, nb, fl in (("affine_fixed", f_fix, 4096, box_flop(3)),
-                            ("affine_truncate256", f_tr, 1024, box_flop(3, 256))):
-        cc, vvv = c[:nb].contiguous(), vv[:nb].contiguous()
-        _, t = timed(lambda: f.bounds_general_box(params, cc, vvv), max(1, args.steps // 2), 1)
-        tf = nb * fl / t / 1e12
-        rows[name] = {"boxes_per_s": nb / t, "ms": t * 1e3, "boxes": nb, "flop_per_box": fl,
-                      "achieved_tflops": tf, "fp32_fma_peak_tflops": peak, "frac": tf / peak}
-    out["classify"] = rows
-    out["value"] = out["affine_fixed_1024x1024"]["rays_per_s"]
-    out["unit"] = "rays/s"
+    nb = 1024
+    c = torch.from_numpy(rng.uniform(-0.8, 0.8, (nb, 3)).astype(np.float32)).cuda()
+    vv = torch.from_numpy(np.tile((0.01 * np.eye(3, dtype=np.float32))[None], (nb, 1, 1))).cuda()
+    peak32 = fp32_peak_tflops(torch.cuda.current_device())
+    peaks = measured_peaks()
+    tf32_peak = peaks.get('bf16_tflops', 1900.) / 2
+    forms = [("affine_fixed", 'affine_fixed', {}, 'auto', box_flop(3)),
+             ("affine_truncate256_fp32", 'affine_truncate', {'affine_n_truncate': 256}, 'fp32', box_flop(3, 256)),
+             ("affine_truncate256_3xtf32", 'affine_truncate', {'affine_n_truncate': 256}, '3xtf32', box_flop(3, 256))]
+    out = {"metric": "rays/s and bounded boxes/s, ReLU 3x256x8 MLP (32x32 strided rays of 1024^2)",
+           "unit": "rays/s", "config": {"workload": "precision_relu256x8", "rays": int(rs.shape[0]),
+                                        "boxes": nb, "conservative": True}}
+    for name, mode, kw, products, fl in forms:
+        f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=True,
+                                                                    products=products, **kw)
+        r, t = timed(lambda: niq.queries.cast_rays((f,), (params,), rs, ds, opts, return_device=True), 1, 1)
+        _, tb = timed(lambda: f.bounds_general_box(params, c, vv), 3, 1)
+        tf = nb * fl / tb / 1e12
+        row = {"rays_per_s": rs.shape[0] / t, "cast_ms": t * 1e3, "ray_steps": int(r[2].sum().item()),
+               "hits": int((r[1] > 0).sum().item()), "boxes_per_s": nb / tb, "classify_ms": tb * 1e3,
+               "flop_per_box": fl, "achieved_tflops": tf}
+        if products == '3xtf32':
+            row["tensor_tflops"] = 3 * tf
+            row["roofline"] = {"bound": "tensor", "achieved": 3 * tf, "peak": tf32_peak, "unit": "TFLOP/s",
+                               "frac": 3 * tf / tf32_peak,
+                               "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json)"}
+        else:
+            row["roofline"] = {"bound": "fp32", "achieved": tf, "peak": peak32, "unit": "TFLOP/s", "frac": tf / peak32}
+        out[name] = row
+    out["value"] = out["affine_truncate256_3xtf32"]["rays_per_s"]
+    out["tensor_vs_fp32_classify"] = out["affine_truncate256_3xtf32"]["boxes_per_s"] / \
+        out["affine_truncate256_fp32"]["boxes_per_s"]
     print(json.dumps(out))
 
 
@@ -553,14 +557,17 @@ def run_serve(args):
     errors = sum(1 for f in futs if f.exception(timeout=1800) is not None)
     t_sat = time.perf_counter() - t0
     peak = len(sat) / t_sat
+    st_sat = srv.stats()
     srv.latencies.clear()
+    srv.kind_latencies.clear()
     out = {"metric": "served requests/s and p50/p99 latency (64 resident MLPs, mixed requests)",
            "unit": "requests/s", "saturation": {"requests": len(sat), "seconds": t_sat, "req_per_s": peak,
-                                                 "errors": errors}, "rates": []}
+                                                 "errors": errors, "by_kind": st_sat.get("by_kind")}, "rates": []}
     for frac in args.serve_fracs:
         rate = frac * peak
         reqs = make_serving_requests(niq, max(8, int(rate * args.serve_seconds)), rng, max_res=args.serve_max_res)
         srv.latencies.clear()
+        srv.kind_latencies.clear()
         gaps = rng.exponential(1.0 / rate, len(reqs))
         t_start = time.perf_counter()
         t_next = t_start
@@ -576,7 +583,7 @@ def run_serve(args):
         st = srv.stats()
         out["rates"].append({"fraction_of_peak": frac, "offered_req_per_s": rate, "completed": st.get("completed", 0),
                              "achieved_req_per_s": len(reqs) / t_all, "p50_ms": st.get("p50_ms"),
-                             "p99_ms": st.get("p99_ms"), "errors": errs})
+                             "p99_ms": st.get("p99_ms"), "errors": errs, "by_kind": st.get("by_kind")})
     srv.close()
     seventy = [r for r in out["rates"] if abs(r["fraction_of_peak"] - 0.7) < 1e-6]
     out["value"] = peak

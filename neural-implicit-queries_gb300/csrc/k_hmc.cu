@@ -146,7 +146,7 @@ struct HmcArgs {
 };
 
 template <int TPI>
-__global__ void __launch_bounds__(kNT, 2) k_hmc(NiqModelRef M, HmcArgs a, unsigned long long* grab, int fixed_floats,
+__global__ void __launch_bounds__(kNT) k_hmc(NiqModelRef M, HmcArgs a, unsigned long long* grab, int fixed_floats,
                                              int sw_cap, int resident) {
     using Cfg = TileCfg<8, 0, TPI, kNT>;
     constexpr int ITEMS = Cfg::ITEMS, R = Cfg::R, LD = Cfg::LD;

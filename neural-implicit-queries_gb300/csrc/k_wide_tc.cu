@@ -26,8 +26,9 @@
 // in tf32, the lo parts lose at most 2^-10 of themselves (2^-20 of x or a), the dropped
 // lo*lo term is below 2^-20 |x||a|, and the fp32 accumulation is charged 2^-21 per
 // addition (four times the unit of a truncating fp32 adder).  As in the FP32 engine the
-// bound is charged to err before the layer (err_k += gamma_tc * sum_r |X_rk|, bounded by
-// alpha_k S_k + delta_k) and travels through err @ |A|.
+// per-neuron bound rho_j = (gamma |base| + gamma_tc sum_r |X_r|) @ |A| (sum_r |X_rk| is
+// bounded by alpha_k S_k + delta_k) widens the bounds that choose the linearisation and
+// joins neuron j's new noise row, so it travels through later layers with A, not |A|.
 #include <mutex>
 #include "wide_engine.cuh"
 #include "tc_sm100.cuh"
@@ -46,7 +47,7 @@ constexpr long long kTcPolls = 1ll << 24;      // mbarrier polls before a wait g
 constexpr int kTcOffTr = 2 * kTcStage;
 constexpr int kTcOffPart = kTcOffTr + kTcRows * kTcTrLD;
 constexpr int kTcOffVec = kTcOffPart + 256;
-constexpr int kTcOffMag = kTcOffVec + 6 * 256;
+constexpr int kTcOffMag = kTcOffVec + 8 * 256;
 constexpr int kTcOffRank = kTcOffMag + 512;
 constexpr int kTcSmemFloats = kTcOffRank + 512;
 constexpr size_t kTcSmemBytes = (size_t)kTcSmemFloats * 4;
@@ -119,6 +120,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     float* s_alpha = s_S + 256;
     float* s_delta = s_alpha + 256;
     float* s_drop = s_delta + 256;
+    float* s_rho = s_drop + 256;    // rounding bound of the layer's dot products, per neuron
+    float* s_fold = s_rho + 256;    // per input k: the bound's share before |A| (conservative)
     float* s_mag = smem + kTcOffMag;
     int* s_rank = reinterpret_cast<int*>(smem + kTcOffRank);
     __shared__ NiqSpecHeader H;
@@ -163,28 +166,29 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             const NiqLayer L = H.layers[0];
             const float* A = a.M.w + L.a_off;
             const float g0 = C ? L.gamma : 0.f;
-            float c[3], er[3];
+            float c[3], fo[3];
             for (int k = 0; k < 3; ++k) {
                 c[k] = a.center[3 * b + k];
                 float S = fabsf(c[k]);
                 for (int r = 0; r < v; ++r) S = __fadd_ru(S, fabsf(a.vecs[3 * v * b + 3 * r + k]));
-                er[k] = C ? __fmul_ru(g0, S) : 0.f;
+                fo[k] = C ? __fmul_ru(g0, S) : 0.f;
             }
             if (tid < NIQ_MAX_WIDTH) {
                 const int j = tid;
-                float bs = 0.f, es = 0.f;
+                float bs = 0.f, rho = 0.f;
                 if (j < L.out) {
                     for (int k = 0; k < 3; ++k) {
                         const float w = A[k * L.out_pad + j];
                         bs = fmaf(c[k], w, bs);
-                        es = fmaf(er[k], fabsf(w), es);
+                        if (C) rho = __fmaf_ru(fo[k], fabsf(w), rho);
                     }
                     const float bj = a.M.w[L.b_off + j];
                     bs = __fadd_rn(bs, bj);
-                    if (C) es = __fadd_ru(__fmaf_ru(es, 1.f + 2.f * g0, __fmul_ru(g0, fabsf(bj))), 5.f * NIQ_TINY);
+                    if (C) rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * g0, __fmul_ru(g0, fabsf(bj))), 5.f * NIQ_TINY);
                 }
                 s_base[j] = bs;
-                s_err[j] = es;
+                s_err[j] = 0.f;   // the input box has no err term
+                s_rho[j] = rho;
             }
             // noise rows r < v: D_rj = vecs_r . A[:, j] into TMEM lane r (warp 0, tile 0)
             if (warp == 0) {
@@ -274,22 +278,25 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         // base and err rows while the tensor cores work (src/affine_layers.py:11-31)
                         const float* A = a.M.w + L.a_off;
                         const float gam = C ? L.gamma : 0.f;
-                        float bs = 0.f, es = 0.f;
+                        float bs = 0.f, es = 0.f, rho = 0.f;
                         const int j = tid;
                         if (j < out) {
                             for (int k = 0; k < L.in; ++k) {
                                 const float w = __ldg(A + k * L.out_pad + j);
                                 bs = fmaf(s_base[k], w, bs);
                                 es = fmaf(s_err[k], fabsf(w), es);
+                                if (C) rho = __fmaf_ru(s_fold[k], fabsf(w), rho);
                             }
                             const float bj = a.M.w[L.b_off + j];
                             bs = __fadd_rn(bs, bj);
-                            if (C)
-                                es = __fadd_ru(__fmaf_ru(es, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))),
-                                               (float)(L.in + 2) * NIQ_TINY);
+                            if (C) {
+                                es = __fmul_ru(es, 1.f + 2.f * gam);
+                                rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))),
+                                                (float)(L.in + 2) * NIQ_TINY);
+                            }
                         }
                         __syncthreads();  // every thread read the old vectors
-                        if (j < NIQ_MAX_WIDTH) { s_base[j] = bs; s_err[j] = es; }
+                        if (j < NIQ_MAX_WIDTH) { s_base[j] = bs; s_err[j] = es; s_rho[j] = rho; }
                     }
                 }
                 // every MMA of the layer complete before TMEM is read; a wait that gave up
@@ -322,7 +329,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             float nb = 0.f, e = 0.f, aS = 0.f, alpha = 0.f, delta = 0.f;
             if (j < out) {
                 const float base = s_base[j], err = s_err[j], S = s_S[j];
-                const float rad = add_up<C>(S, err);
+                const float rad = add_up<C>(add_up<C>(S, err), s_rho[j]);
                 const float lo = sub_dn<C>(base, rad), hi = add_up<C>(base, rad);
                 const Lin z = linearize<C>(L.act, lo, hi);
                 alpha = z.a;
@@ -330,7 +337,11 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 nb = C ? fmaf(z.a, base, z.b) : __fadd_rn(__fmul_rn(z.a, base), z.b);
                 aS = C ? __fmul_ru(__fmul_ru(z.a, S), 1.f + NIQ_ULP_REL) : 0.f;
                 e = C ? __fmul_ru(z.a, err) : __fmul_rn(z.a, err);
-                if (C) e = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, e);
+                if (C) {
+                    // neuron j's symbol: linearisation, the layer's rounding, alpha*base + beta, alpha*aff
+                    delta = __fmaf_ru(z.a, s_rho[j], delta);
+                    delta = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, delta);
+                }
             }
             if (j < NIQ_MAX_WIDTH) { s_alpha[j] = alpha; s_delta[j] = delta; }
             __syncthreads();
@@ -417,21 +428,21 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             }
             __syncthreads();
             // 6. err of the activation output, with the next layer's rounding folded in
+            float fold = 0.f;
             if (j < out) {
                 e = add_up<C>(e, s_drop[j]);
                 if (C) {
                     const NiqLayer& Ln = H.layers[li + 1];
-                    if (li + 2 < nL) {  // next layer on the tensor cores, base on the CUDA cores
-                        e = __fmaf_ru(Ln.gamma, fabsf(nb), e);
-                        e = __fmaf_ru(gamma_tc(Ln.in), __fadd_ru(aS, delta), e);
-                    } else {
-                        e = __fmaf_ru(Ln.gamma, __fadd_ru(__fadd_ru(fabsf(nb), aS), delta), e);
-                    }
+                    if (li + 2 < nL)  // next layer: noise rows on the tensor cores, base on the CUDA cores
+                        fold = __fmaf_ru(gamma_tc(Ln.in), __fadd_ru(aS, delta), __fmul_ru(Ln.gamma, fabsf(nb)));
+                    else
+                        fold = __fmul_ru(Ln.gamma, __fadd_ru(__fadd_ru(fabsf(nb), aS), delta));
                 }
             }
             if (j < NIQ_MAX_WIDTH) {
                 s_base[j] = j < out ? nb : 0.f;
                 s_err[j] = j < out ? e : 0.f;
+                s_fold[j] = fold;
             }
             nrows = keep;
             // X written by this layer visible to the next layer's copies; TMEM reads done
@@ -461,16 +472,20 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             }
             const float S = wide_block_sum<C>(part_s, red);
             if (tid == 0) {
-                float bs = 0.f, es = 0.f;
+                float bs = 0.f, es = 0.f, rho = 0.f;
                 for (int k = 0; k < L.in; ++k) {
                     const float w = A[k * L.out_pad];
                     bs = fmaf(s_base[k], w, bs);
                     es = fmaf(s_err[k], fabsf(w), es);
+                    if (C) rho = __fmaf_ru(s_fold[k], fabsf(w), rho);
                 }
                 const float bj = a.M.w[L.b_off];
                 bs = __fadd_rn(bs, bj);
-                if (C) es = __fadd_ru(__fmaf_ru(es, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))), (float)(L.in + 2) * NIQ_TINY);
-                const float rad = add_up<C>(S, es);
+                if (C) {
+                    es = __fmul_ru(es, 1.f + 2.f * gam);
+                    rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))), (float)(L.in + 2) * NIQ_TINY);
+                }
+                const float rad = add_up<C>(add_up<C>(S, es), rho);
                 const float lo = sub_dn<C>(bs, rad), hi = add_up<C>(bs, rad);
                 a.sign_out[b] = sign_of_bounds(lo, hi, a.offset);
                 if (a.lohi_out) { a.lohi_out[2 * b] = lo; a.lohi_out[2 * b + 1] = hi; }
@@ -556,8 +571,11 @@ bool wide_tc_eligible(const NiqSpecHeader& H, const niq_bound_opts& o, int v) {
 
 bool wide_use_tc(const NiqSpecHeader& H, const niq_bound_opts& o, int v) {
     if (o.products == NIQ_PRODUCTS_FP32 || !wide_tc_eligible(H, o, v)) return false;
-    // automatic selection stays on FP32 FMA until the tensor-core form is measured
-    return o.products == NIQ_PRODUCTS_3XTF32;
+    if (o.products == NIQ_PRODUCTS_3XTF32) return true;
+    // automatic: the tensor cores pay off when rows x width is dense (measured 5.3x the FP32
+    // engine on 256 rows of a 256-wide network)
+    const int rows = o.mode == NIQ_MODE_AFFINE_TRUNCATE ? o.truncate_count : wide_rows_cap(H, o, v);
+    return H.max_width >= 128 && rows >= 64;
 }
 
 size_t wide_tc_workspace_bytes() {

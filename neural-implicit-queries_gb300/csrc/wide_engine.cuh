@@ -9,6 +9,14 @@
 // keeps the first truncate_count, folding the rest into err; 'append' keeps the
 // n_append largest deltas as new rows (ties to the lower index, as lax.top_k) and adds
 // the remainder, as one scalar, to every err entry (src/affine.py:183-191).
+//
+// Conservative mode.  The rounding error of a layer's dot products (at most gamma times
+// |base| + sum_r |aff_r| pushed through |A|, plus the bias addition) is a per-neuron
+// quantity rho_j.  These modes give it its own noise symbol: it widens the bounds that
+// choose the linearisation, and alpha_j rho_j joins neuron j's new noise row delta_j
+// (together with the rounding of alpha*base + beta and alpha*aff).  A symbol travels
+// through the next layers with A, not |A| as err does, so the outward terms stay
+// proportional to the values instead of growing like |A|^depth.
 #pragma once
 #include "niq_host.cuh"
 
@@ -79,6 +87,7 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
     __shared__ float xin[kWideRB][NIQ_MAX_WIDTH + 4];
     __shared__ float red[40];
     __shared__ float sdelta[NIQ_MAX_WIDTH];
+    __shared__ float sfold[NIQ_MAX_WIDTH];   // gamma (|base_k| + sum_r |aff_rk|) before the layer (conservative)
     load_header(H, M.hdr);
     __syncthreads();
     const int W = H.max_width;
@@ -106,7 +115,8 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
                 cur[(2 + r) * W + k] = a;
                 S = __fadd_ru(S, fabsf(a));
             }
-            cur[W + k] = C ? __fmul_ru(H.layers[0].gamma, S) : 0.f;
+            cur[W + k] = 0.f;
+            sfold[k] = C ? __fmul_ru(H.layers[0].gamma, S) : 0.f;
         }
         __syncthreads();
         for (int li = 0; li < H.n_layers; ++li) {
@@ -141,19 +151,29 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
                         float val = acc[rr];
                         if (j >= L.out) val = 0.f;
                         else if (row == 0) val = __fadd_rn(val, bj);
-                        else if (row == 1 && C)
-                            val = __fadd_ru(__fmaf_ru(val, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))), (float)(L.in + 2) * NIQ_TINY);
+                        else if (row == 1 && C) val = __fmul_ru(val, 1.f + 2.f * gam);
                         nxt[(long long)row * W + j] = val;
                     }
                 }
                 __syncthreads();
             }
+            // rounding bound of this layer's dot products and bias addition, per neuron
+            float rho = 0.f;
+            if (C && j < L.out) {
+                for (int k = 0; k < L.in; ++k) rho = __fmaf_ru(sfold[k], fabsf(__ldg(A + k * L.out_pad + j)), rho);
+                rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))), (float)(L.in + 2) * NIQ_TINY);
+            }
             float* t = cur; cur = nxt; nxt = t;   // cur: this layer's output
+            __syncthreads();  // every thread has read sfold
             if (L.act == NIQ_ACT_NONE) {
-                if (C && li + 1 < H.n_layers && j < L.out) {
-                    float S = 0.f;
-                    for (int r = 0; r < nrows; ++r) S = __fadd_ru(S, fabsf(cur[(long long)(2 + r) * W + j]));
-                    cur[W + j] = __fmaf_ru(H.layers[li + 1].gamma, __fadd_ru(fabsf(cur[j]), S), cur[W + j]);
+                // no new symbol without an activation: the rounding goes to err
+                if (C && j < L.out) {
+                    cur[W + j] = __fadd_ru(cur[W + j], rho);
+                    if (li + 1 < H.n_layers) {
+                        float S = 0.f;
+                        for (int r = 0; r < nrows; ++r) S = __fadd_ru(S, fabsf(cur[(long long)(2 + r) * W + j]));
+                        sfold[j] = __fmul_ru(H.layers[li + 1].gamma, __fadd_ru(fabsf(cur[j]), S));
+                    }
                 }
                 __syncthreads();
                 continue;
@@ -165,7 +185,7 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
                 float S = 0.f;
                 for (int r = 0; r < nrows; ++r) S = add_up<C>(S, fabsf(cur[(long long)(2 + r) * W + j]));
                 const float base = cur[j], err = cur[W + j];
-                const float rad = add_up<C>(S, err);
+                const float rad = add_up<C>(add_up<C>(S, err), rho);
                 const float lo = sub_dn<C>(base, rad), hi = add_up<C>(base, rad);
                 const Lin z = linearize<C>(L.act, lo, hi);
                 alpha = z.a;
@@ -176,10 +196,13 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
                 }
                 delta_j = fabsf(z.d);
                 aS = C ? __fmul_ru(__fmul_ru(z.a, S), 1.f + NIQ_ULP_REL) : 0.f;
-                float e = C ? __fmul_ru(z.a, err) : __fmul_rn(z.a, err);
-                if (C) e = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, e);
+                if (C) {
+                    // neuron j's symbol: linearisation, this layer's rounding, alpha*base + beta and alpha*aff
+                    delta_j = __fmaf_ru(z.a, rho, delta_j);
+                    delta_j = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, delta_j);
+                }
                 cur[j] = nb;
-                cur[W + j] = e;
+                cur[W + j] = C ? __fmul_ru(z.a, err) : __fmul_rn(z.a, err);
             }
             if (mode == NIQ_MODE_AFFINE_APPEND) {
                 if (j < NIQ_MAX_WIDTH) sdelta[j] = (j < L.out) ? delta_j : -INFINITY;
@@ -196,9 +219,8 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
                     if (j < L.out_pad) cur[(long long)(2 + nrows + r) * W + j] = (j < L.out && rk == r) ? delta_j : 0.f;
                 if (j < L.out) {
                     const float rest = C ? __fsub_ru(dsum, ksum) : dsum - ksum;
-                    float e = add_up<C>(cur[W + j], rest);
-                    if (C) e = __fmaf_ru(gam_next, __fadd_ru(__fadd_ru(fabsf(cur[j]), aS), delta_j), e);
-                    cur[W + j] = e;
+                    cur[W + j] = add_up<C>(cur[W + j], rest);
+                    if (C) sfold[j] = __fmul_ru(gam_next, __fadd_ru(__fadd_ru(fabsf(cur[j]), aS), delta_j));
                 }
                 nrows += k;
                 __syncthreads();
@@ -207,7 +229,7 @@ __global__ void __launch_bounds__(kWideNT) k_wide_classify(NiqModelRef M, niq_bo
             // 'affine_all' / 'affine_truncate': append diag(delta)
             for (int r = 0; r < L.out; ++r)
                 if (j < L.out_pad) cur[(long long)(2 + nrows + r) * W + j] = (j == r) ? delta_j : 0.f;
-            if (C && j < L.out) cur[W + j] = __fmaf_ru(gam_next, __fadd_ru(__fadd_ru(fabsf(cur[j]), aS), delta_j), cur[W + j]);
+            if (C && j < L.out) sfold[j] = __fmul_ru(gam_next, __fadd_ru(__fadd_ru(fabsf(cur[j]), aS), delta_j));
             nrows += L.out;
             __syncthreads();
             if (mode == NIQ_MODE_AFFINE_TRUNCATE && nrows > opts.truncate_count) {

@@ -100,6 +100,7 @@ class Server:
         self._lock = threading.Condition()
         self._stop = False
         self.latencies = []
+        self.kind_latencies = collections.defaultdict(list)
         self.completed = 0
         self.budget_exhausted = 0   # closest-point launches in which a query spent its node budget
         self._sched = threading.Thread(target=self._schedule, daemon=True)
@@ -127,9 +128,12 @@ class Server:
         lat = np.array(self.latencies) * 1e3
         if lat.size == 0:
             return {"completed": 0}
+        per_kind = {k: {"n": len(v), "p50_ms": float(np.percentile(np.array(v) * 1e3, 50)),
+                        "p99_ms": float(np.percentile(np.array(v) * 1e3, 99))}
+                    for k, v in self.kind_latencies.items() if v}
         return {"completed": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                "closest_budget_exhausted": self.budget_exhausted}
+                "closest_budget_exhausted": self.budget_exhausted, "by_kind": per_kind}
 
     # ------------------------------------------------------------------ scheduler
     def _next_stream(self):
@@ -238,6 +242,7 @@ class Server:
         with self._lock:
             self._inflight_bytes -= p.bytes
             self.latencies.append(now - p.t_submit)
+            self.kind_latencies['intersect'].append(now - p.t_submit)
             self.completed += 1
             self._lock.notify_all()
         if exc is not None:
@@ -312,6 +317,7 @@ class Server:
             for p, r in zip(pend, results):
                 self._inflight_bytes -= p.bytes
                 self.latencies.append(now - p.t_submit)
+                self.kind_latencies[kind].append(now - p.t_submit)
                 self.completed += 1
             self._lock.notify_all()
         for p, r in zip(pend, results):

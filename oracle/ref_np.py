@@ -604,6 +604,140 @@ def look_at(eye_pos, target=None, up_dir='y', dtype=np.float32):
     return look.astype(dtype), up.astype(dtype), left.astype(dtype)
 
 
+def camera_ray(look_dir, up_dir, left_dir, fov_x, fov_y, theta_x, theta_y, dtype=np.float32):
+    """src/render.py:17-23, batched over theta_x/theta_y (image coords on [-1, 1])."""
+    tx = np.asarray(np.tan(np.deg2rad(np.asarray(fov_x, dtype)) / 2), dtype)
+    ty = np.asarray(np.tan(np.deg2rad(np.asarray(fov_y, dtype)) / 2), dtype)
+    p = (look_dir[None, :] + left_dir[None, :] * (theta_x * tx)[:, None]
+         + up_dir[None, :] * (theta_y * ty)[:, None]).astype(dtype)
+    return normalize(p).astype(dtype)
+
+
+def _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32):
+    """The substep loop of one cast_rays_frustum iteration for a batch of frusta
+    (src/queries.py:202-321): returns (t, step_size, is_hit, hit_id, demands_subd, steps)."""
+    root, look, up, left, fov_x, fov_y, res_x, res_y = cam
+    x_lo, y_lo, x_hi, y_hi = rng_[:, 0], rng_[:, 1], rng_[:, 2], rng_[:, 3]
+    single = (x_lo + 1 == x_hi) & (y_lo + 1 == y_hi)
+    rx1, ry1 = np.asarray(res_x + 1., f32), np.asarray(res_y + 1., f32)
+    xc_lo = (np.asarray(2., f32) * x_lo.astype(f32) / rx1 - 1).astype(f32)
+    xc_hi = (np.asarray(2., f32) * (x_hi - 1).astype(f32) / rx1 - 1).astype(f32)
+    yc_lo = (np.asarray(2., f32) * y_lo.astype(f32) / ry1 - 1).astype(f32)
+    yc_hi = (np.asarray(2., f32) * (y_hi - 1).astype(f32) / ry1 - 1).astype(f32)
+    ray = lambda a, b: camera_ray(look, up, left, fov_x, fov_y, a, b, f32)
+    r_uu, r_lu, r_ul = ray(xc_hi, yc_hi), ray(xc_lo, yc_hi), ray(xc_hi, yc_lo)
+    r_ll = ray(xc_lo, yc_lo)
+    mid = (np.asarray(0.5, f32) * (r_uu + r_ll)).astype(f32)
+    mid_len = np.linalg.norm(mid, axis=-1).astype(f32)
+    mid = (mid / mid_len[:, None]).astype(f32)
+    expand = (np.asarray(1., f32) / mid_len).astype(f32)
+    n = t.shape[0]
+    is_hit = np.zeros(n, bool)
+    hit_id = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int32)
+    demands = np.zeros(n, bool)
+    hit_eps = np.asarray(opts['hit_eps'], f32)
+    for _ in range(opts['n_substeps']):
+        t_up = (t + size).astype(f32)
+        t_adj = (t_up * expand).astype(f32)
+        right_front = ((r_uu - r_lu) * t_adj[:, None] / 2).astype(f32)
+        up_front = ((r_uu - r_ul) * t_adj[:, None] / 2).astype(f32)
+        can_step = ~is_hit
+        steps += (~is_hit).astype(np.int32)
+        center = (root[None, :] + (np.asarray(0.5, f32) * (t + t_adj))[:, None] * mid).astype(f32)
+        cvec = ((np.asarray(0.5, f32) * (t_adj - t))[:, None] * mid).astype(f32)
+        vecs = np.stack((cvec, right_front, up_front), axis=1)
+        for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
+            btype = func.classify_general_box(params, center, vecs)
+            can_step &= (btype == SIGN_POSITIVE) | (btype == SIGN_NEGATIVE)
+            p0 = (root[None, :] + t[:, None] * mid).astype(f32)
+            p1 = (root[None, :] + (t + hit_eps)[:, None] * mid).astype(f32)
+            this_hit = np.sign(func(params, p0)) != np.sign(func(params, p1))
+            hit_id = np.where(this_hit, fid, hit_id).astype(np.int32)
+            is_hit |= this_hit
+        this_step = np.where(can_step, size, hit_eps * single.astype(f32)).astype(f32)
+        t = np.where(is_hit, t, t + this_step * np.asarray(opts['safety_factor'], f32)).astype(f32)
+        size = np.where(can_step, size * np.asarray(opts['interval_grow_fac'], f32),
+                        size * np.asarray(opts['interval_shrink_fac'], f32)).astype(f32)
+        demands = demands | (size < hit_eps) | is_hit
+        size = np.maximum(size, hit_eps).astype(f32)
+    return t, size, is_hit, hit_id, demands, steps
+
+
+def cast_rays_frustum(funcs, params_list, cam_params, opts):
+    """src/queries.py:178-587: frusta over integer pixel ranges march like rays with a
+    3-vector box (the frustum's extent at the far end of the step), split in half along
+    the wider axis when the step size falls behind the frustum's width, and hit only as
+    single pixels.  Returns (out_t, out_hit_id, out_count, n_frustum_steps) with the
+    outputs indexed [x, y] as the reference writes them.  The reference's buckets and
+    compaction do not change any frustum's result; the frusta are kept compact here."""
+    f32 = funcs[0].dtype
+    root, look, up, left, fov_x, fov_y, res_x, res_y = cam_params
+    cam = (np.asarray(root, f32), np.asarray(look, f32), np.asarray(up, f32), np.asarray(left, f32),
+           float(fov_x), float(fov_y), int(res_x), int(res_y))
+    ns = int(opts['n_side_init'])
+    xt = jax_linspace(0., float(res_x), ns + 1, np.float32).astype(np.int64)
+    yt = jax_linspace(0., float(res_y), ns + 1, np.float32).astype(np.int64)
+    rng_ = np.stack((np.tile(xt[:-1], ns), np.repeat(yt[:-1], ns), np.tile(xt[1:], ns), np.repeat(yt[1:], ns)), -1)
+    t = np.zeros(ns * ns, f32)
+    size = (np.ones(ns * ns, f32) * np.asarray(opts['interval_init_size'], f32) *
+            np.asarray(opts['max_dist'], f32)).astype(f32)
+    count = np.zeros(ns * ns, f32)
+    fin = []
+    it = 0
+    n_steps = 0
+    fov_x_rad = np.asarray(np.deg2rad(np.asarray(fov_x, f32)), f32)
+    fov_y_rad = np.asarray(np.deg2rad(np.asarray(fov_y, f32)), f32)
+    while rng_.shape[0]:
+        n_steps += rng_.shape[0]
+        t, size, is_hit, hit_id, demands, steps = _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32)
+        area = ((rng_[:, 2] - rng_[:, 0]) * (rng_[:, 3] - rng_[:, 1])).astype(np.int64)
+        count = (count + steps.astype(f32) * (np.asarray(1., f32) / area.astype(f32))).astype(f32)
+        is_hit = is_hit & (area == 1)
+        term = is_hit | (t > opts['max_dist']) | (it >= opts['n_max_step'])
+        if term.any():
+            fin.append((rng_[term], t[term], hit_id[term], count[term]))
+        keep = ~term
+        rng_, t, size, count, demands = rng_[keep], t[keep], size[keep], count[keep], demands[keep]
+        it += opts['n_substeps']
+        if not rng_.shape[0]:
+            break
+        xw = (rng_[:, 2] - rng_[:, 0]).astype(f32)
+        yw = (rng_[:, 3] - rng_[:, 1]).astype(f32)
+        wx = (np.asarray(2., f32) * np.sin(fov_x_rad / 2 * xw / np.asarray(res_x, f32)).astype(f32) * t).astype(f32)
+        wy = (np.asarray(2., f32) * np.sin(fov_y_rad / 2 * yw / np.asarray(res_y, f32)).astype(f32) * t).astype(f32)
+        can = (rng_[:, 2] > rng_[:, 0] + 1) | (rng_[:, 3] > rng_[:, 1] + 1)
+        rf = np.asarray(opts['refine_width_fac'], f32)
+        refine = ((wx > rf * size) | (wy > rf * size) | demands) & can
+        if refine.any():                                    # subdivide_frusta, :409-467
+            sub = rng_[refine]
+            subd_x = (sub[:, 2] - sub[:, 0]) >= (sub[:, 3] - sub[:, 1])
+            xm = (sub[:, 0] + sub[:, 2]) // 2
+            ym = (sub[:, 1] + sub[:, 3]) // 2
+            a = sub.copy()
+            a[:, 2] = np.where(subd_x, xm, sub[:, 2])
+            a[:, 3] = np.where(~subd_x, ym, sub[:, 3])
+            b = sub.copy()
+            b[:, 0] = np.where(subd_x, xm, sub[:, 0])
+            b[:, 1] = np.where(~subd_x, ym, sub[:, 1])
+            rng_ = rng_.copy()
+            rng_[refine] = a
+            rng_ = np.concatenate((rng_, b))
+            t = np.concatenate((t, t[refine]))
+            size = np.concatenate((size, size[refine]))
+            count = np.concatenate((count, count[refine]))
+    out_t = np.zeros((int(res_x), int(res_y)), f32)
+    out_hit = np.zeros((int(res_x), int(res_y)), np.int32)
+    out_count = np.zeros((int(res_x), int(res_y)), np.int32)
+    for r_, tt, hh, cc in fin:                              # subdivide to pixels + write, :469-587
+        for i in range(r_.shape[0]):
+            x0, y0, x1, y1 = r_[i]
+            out_t[x0:x1, y0:y1] = tt[i]
+            out_hit[x0:x1, y0:y1] = hh[i]
+            out_count[x0:x1, y0:y1] = np.trunc(cc[i]).astype(np.int32)
+    return out_t, out_hit, out_count, n_steps
+
+
 # ----------------------------------------------------------------------------------------
 # Level-set kd-tree  (src/kd_tree.py:19-218)
 # ----------------------------------------------------------------------------------------

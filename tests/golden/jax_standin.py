@@ -153,7 +153,15 @@ class _AtRef:
         out = self.arr[clipped]
         if mode in ('fill', 'drop') and mask is not None and not mask.all():
             if fill_value is None:
-                fill_value = np.nan if np.issubdtype(out.dtype, np.inexact) else np.iinfo(out.dtype).min
+                # jax's gather fill: NaN for floats, min for signed, max for unsigned, True for bool
+                if np.issubdtype(out.dtype, np.inexact):
+                    fill_value = np.nan
+                elif out.dtype == np.bool_:
+                    fill_value = True
+                elif np.issubdtype(out.dtype, np.unsignedinteger):
+                    fill_value = np.iinfo(out.dtype).max
+                else:
+                    fill_value = np.iinfo(out.dtype).min
             out = np.array(out)
             bad = ~mask
             out[bad] = np.asarray(fill_value).astype(out.dtype)

@@ -53,6 +53,7 @@ def rand_boxes(rng, n, v):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default='/root/reference')
+    ap.add_argument('--only', default=None, help='write one fixture only (e.g. frustum)')
     args = ap.parse_args()
     jax_standin.install()
     sys.path.insert(0, os.path.join(args.reference, 'src'))
@@ -72,6 +73,9 @@ def main():
         'relu32x3': workloads.plain_small_model(),
     }
     t0 = time.time()
+    if args.only == 'frustum':
+        frustum_fixture(queries, load_as_reference, models, t0)
+        return
 
     # ---------------------------------------------------------------- point evals + bounds
     mode_kw = {'interval': {}, 'affine_fixed': {}, 'affine_all': {},
@@ -204,6 +208,36 @@ def main():
         print(f'cp B{B_} {time.time() - t0:.1f}s', flush=True)
     np.savez_compressed(os.path.join(HERE, 'queries.npz'), **out)
     print(f'all done {time.time() - t0:.1f}s')
+
+
+def frustum_fixture(queries, load_as_reference, models, t0):
+    """cast_rays_frustum (src/queries.py:178-587) on the 3x32x3 ReLU model: a 12x10 image,
+    2x2 initial frusta, 32 steps; affine_fixed alone and with two functions and two
+    substeps (the stand-in runs every frustum through Python, so the image is small)."""
+    import jax.numpy as jnp
+    out = {}
+    params = models['relu32x3']
+    out.update(flat('model/relu32x3', params))
+    out.update(flat('model/relu16', models['relu16']))
+    eye = np.array([0., 0., 3.], np.float32)
+    look, up, left = (np.array(v, np.float32) for v in ([0, 0, -1.], [0, 1., 0], [-1., 0, 0]))
+    for name, fs, n_sub in (('one', ('relu32x3',), 1), ('two', ('relu32x3', 'relu16'), 2)):
+        funcs, ps = [], []
+        for m in fs:
+            f, p = load_as_reference(models[m], m, 'affine_fixed')
+            funcs.append(f)
+            ps.append(p)
+        opts = queries.get_default_cast_opts()
+        opts['n_max_step'] = 32
+        opts['n_side_init'] = 2
+        opts['n_substeps'] = n_sub
+        cam = (jnp.array(eye), jnp.array(look), jnp.array(up), jnp.array(left), 40., 30., 12, 10)
+        t, hid, cnt, nev = queries.cast_rays_frustum(tuple(funcs), tuple(ps), cam, opts)
+        out[f'frustum/{name}/t'], out[f'frustum/{name}/hit_id'] = np.asarray(t), np.asarray(hid)
+        out[f'frustum/{name}/count'] = np.asarray(cnt)
+        print(f'frustum {name} {time.time() - t0:.1f}s', flush=True)
+    out['frustum/cam'] = np.concatenate([eye, look, up, left, [40., 30., 12, 10]]).astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, 'frustum.npz'), **out)
 
 
 def _camera(eye, look, up, res, fov):
