@@ -344,6 +344,22 @@ def run_rays(args):
             res_out[form] = {"rays_per_s": res * res / t, "ms": t * 1e3, "ray_steps_per_s": steps / t,
                              "hits": int((r[1] > 0).sum().item())}
         res_out["persistent_speedup"] = res_out["plain"]["ms"] / res_out["persistent"]["ms"]
+        # the frustum cast of the same image (src/queries.py:178-587), 16x16 initial frusta
+        eye = np.array([0., 0., 3.], np.float32)
+        left = np.cross(look, up).astype(np.float32)
+        cam = (eye, look, up, left, 60., 60., res, res)
+        fo = dict(opts)
+        fo['n_side_init'] = 16
+        for _ in range(max(1, args.warmup)):
+            fr = niq.queries.cast_rays_frustum((f,), (params,), cam, fo)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fr = niq.queries.cast_rays_frustum((f,), (params,), cam, fo)
+        torch.cuda.synchronize()
+        tf_ = (time.perf_counter() - t0) / args.steps
+        res_out["frustum"] = {"pixels_per_s": res * res / tf_, "ms": tf_ * 1e3, "frustum_steps": int(fr[3]),
+                              "hits": int((fr[1] > 0).sum()), "timing": "wall clock incl. host loop and D2H"}
         out["config"][f"{res}x{res}"] = res_out
     out["value"] = out["config"]["1024x1024"]["persistent"]["rays_per_s"]
     print(json.dumps(out))
@@ -420,9 +436,15 @@ def run_precision(args):
     out = {"metric": "rays/s and bounded boxes/s, ReLU 3x256x8 MLP (32x32 strided rays of 1024^2)",
            "unit": "rays/s", "config": {"workload": "precision_relu256x8", "rays": int(rs.shape[0]),
                                         "boxes": nb, "conservative": True}}
+    if args.quick:   # profiling runs: the tensor-core classification only
+        forms = forms[2:]
     for name, mode, kw, products, fl in forms:
         f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=True,
                                                                     products=products, **kw)
+        if args.quick:
+            _, tb = timed(lambda: f.bounds_general_box(params, c, vv), 1, 1)
+            print(json.dumps({"quick": True, "classify_ms": tb * 1e3, "boxes": nb}))
+            return
         r, t = timed(lambda: niq.queries.cast_rays((f,), (params,), rs, ds, opts, return_device=True), 1, 1)
         _, tb = timed(lambda: f.bounds_general_box(params, c, vv), 3, 1)
         tf = nb * fl / tb / 1e12

@@ -149,6 +149,69 @@ int niq_cast_rays_plain(const niq_model* const* models, int32_t nfunc, const niq
                         float* t_out, int32_t* hit_id_out, int32_t* count_out, int64_t* n_evals_out,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- queries.cast_rays_frustum (src/queries.py:178-587) ------------------------------
+ * The camera tuple (root_pos, look_dir, up_dir, left_dir, fov_x, fov_y, res_x, res_y) of
+ * the reference; fov in degrees. */
+typedef struct niq_frustum_camera {
+    float root[3];
+    float look[3];
+    float up[3];
+    float left[3];
+    float fov_x, fov_y;
+    int32_t res_x, res_y;
+} niq_frustum_camera;
+/* Frusta start as an n_side_init^2 grid of pixel tiles, march like rays with a box
+ * enclosing each step, split in half along the wider pixel axis when the step falls
+ * behind the frustum's width (refine_width_fac) and hit only as single pixels.  Outputs
+ * are (res_x, res_y) arrays indexed [x][y] as the reference returns them: t_out, hit_id
+ * (1-based function index, 0 = none) and count (steps per pixel, truncated);
+ * n_evals_out (device int64) counts frustum steps.  One launch per iteration with a
+ * host read of the live count, as the reference's loop.  Modes: interval, affine_fixed,
+ * slope_interval.  workspace: niq_cast_frustum_workspace_size() bytes. */
+size_t niq_cast_frustum_workspace_size(int32_t res_x, int32_t res_y, int32_t n_side_init);
+int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
+                     const niq_frustum_camera* camera, const niq_cast_opts* cast, float refine_width_fac,
+                     int32_t n_side_init, float* t_out, int32_t* hit_id_out, int32_t* count_out,
+                     int64_t* n_evals_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- kd_tree.sample_surface / bulk_properties (src/kd_tree.py:220-292, 804-863) --------
+ * Monte Carlo over the nodes of a level-set tree (device arrays (n, 3) of lower and upper
+ * corners): candidates pick a node uniformly and a point uniformly inside it, from a
+ * counter-based generator seeded by `seed` (the reference draws from JAX's threefry
+ * stream: the same distribution, other samples).
+ * niq_sample_surface keeps points with |f| < width until n_samples are found
+ * (samples_out: device (n_samples, 3)), drawing n_per_round candidates per round for at
+ * most max_rounds rounds (NIQ_ERR_TIMEOUT with *n_found_out < n_samples after that).
+ * niq_bulk_properties: mass and centroid of {f < 0}: the interior nodes exactly, the
+ * boundary nodes by n_sample candidates; mass_centroid_out (host, 4 doubles) = mass,
+ * centroid.  workspace: niq_sample_workspace_size(n_per_round or n_sample) bytes. */
+size_t niq_sample_workspace_size(int64_t n_candidates);
+int niq_sample_surface(const niq_model* model, int64_t n_nodes, const float* node_lower, const float* node_upper,
+                       int64_t n_samples, float width, uint64_t seed, int64_t n_per_round, int32_t max_rounds,
+                       float* samples_out, int64_t* n_found_out, void* workspace, size_t workspace_bytes,
+                       void* stream);
+int niq_bulk_properties(const niq_model* model, int64_t n_interior, const float* interior_lower,
+                        const float* interior_upper, int64_t n_boundary, const float* boundary_lower,
+                        const float* boundary_upper, int64_t n_sample, uint64_t seed, double* mass_centroid_out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- render.outward_normals / shade_image (src/render.py:53-90,152-224) ----------------
+ * Normals by the reference's tetrahedron central differences at the hit positions, for
+ * the function each pixel hit (hit_id 1-based; zero normal for no hit).  hit_pos,
+ * hit_id and normals_out are device arrays of n rows.  workspace:
+ * niq_outward_normals_workspace_size(n) bytes. */
+size_t niq_outward_normals_workspace_size(int64_t n);
+int niq_outward_normals(const niq_model* const* models, int32_t nfunc, int64_t n, const float* hit_pos,
+                        const int32_t* hit_id, float eps, float* normals_out, void* workspace,
+                        size_t workspace_bytes, void* stream);
+/* Shading into a device RGB buffer (n, 3): shading 0 = 'normal', 1 = 'matcap_color' with
+ * matcaps a device array (4, matcap_h, matcap_w, 3) of the r, g, b, k images and colors
+ * a host array (ncolors, 3), one per function.  up_dir is host (3).  Pixels without a
+ * hit are white; tonemap != 0 applies tonemap_image (src/render.py:152-158). */
+int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
+                    const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
+                    const float* colors, int32_t ncolors, int32_t tonemap, float* rgb_out, void* stream);
+
 /* ---- level-set kd-tree: construct_uniform_unknown_levelset_tree
  *      (src/kd_tree.py:19-218) ------------------------------------------------------ *
  * Breadth-first bisection of the box [lower, upper] (host float[3] each) for

@@ -43,6 +43,11 @@ class BoundOpts(C.Structure):
                 ('conservative', C.c_int32), ('products', C.c_int32)]
 
 
+class FrustumCamera(C.Structure):
+    _fields_ = [('root', C.c_float * 3), ('look', C.c_float * 3), ('up', C.c_float * 3), ('left', C.c_float * 3),
+                ('fov_x', C.c_float), ('fov_y', C.c_float), ('res_x', C.c_int32), ('res_y', C.c_int32)]
+
+
 class CastOpts(C.Structure):
     _fields_ = [('hit_eps', C.c_float), ('max_dist', C.c_float), ('n_max_step', C.c_int32),
                 ('n_substeps', C.c_int32), ('safety_factor', C.c_float),
@@ -72,6 +77,17 @@ _SIGS = {
                                       _P, _P, _P, _P, _P, _SZ, _P]),
     'niq_tree_workspace_size': (_SZ, [_I64, _I32]),
     'niq_levelset_tree': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P, _SZ, _P]),
+    'niq_cast_frustum_workspace_size': (_SZ, [_I32, _I32, _I32]),
+    'niq_cast_frustum': (C.c_int, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), C.POINTER(FrustumCamera),
+                                   C.POINTER(CastOpts), _F32, _I32, _P, _P, _P, _P, _P, _SZ, _P]),
+    'niq_sample_workspace_size': (_SZ, [_I64]),
+    'niq_sample_surface': (C.c_int, [_P, _I64, _P, _P, _I64, _F32, C.c_uint64, _I64, _I32, _P, C.POINTER(_I64), _P,
+                                     _SZ, _P]),
+    'niq_bulk_properties': (C.c_int, [_P, _I64, _P, _P, _I64, _P, _P, _I64, C.c_uint64, C.POINTER(C.c_double), _P,
+                                      _SZ, _P]),
+    'niq_outward_normals_workspace_size': (_SZ, [_I64]),
+    'niq_outward_normals': (C.c_int, [C.POINTER(_P), _I32, _I64, _P, _P, _F32, _P, _P, _SZ, _P]),
+    'niq_shade_image': (C.c_int, [_I32, _I64, _P, _P, _P, _PF, _P, _I32, _I32, _PF, _I32, _I32, _P, _P]),
     'niq_levelset_tree_plain': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
                                           _SZ, _P]),
     'niq_tree_result': (C.c_int, [_P, _I64, _I32, _I32, C.POINTER(_P), C.POINTER(_P)]),

@@ -17,23 +17,10 @@
 // has terminated (one launch).  k_rays<PERSISTENT=false>: one reference iteration over a
 // list of live rays, appending survivors to the next list (the plain form).
 #include <vector>
-#include "niq_host.cuh"
+#include "cast_common.cuh"
 #include "wide_engine.cuh"
 
 namespace niq {
-
-constexpr int kMaxFuncs = 8;
-
-struct ModelSet {
-    NiqModelRef m[kMaxFuncs];
-    int woff[kMaxFuncs];   // float offset of each model's weights in the resident buffer
-    int n;
-};
-
-struct CastDev {
-    float hit_eps, max_dist, safety, grow, shrink, init_step;
-    int n_max_step, n_substeps;
-};
 
 struct RayWs {                      // device workspace header
     unsigned long long next_ray;    // persistent: next unclaimed ray
@@ -224,22 +211,6 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
     if (threadIdx.x < S.n && s_evals[threadIdx.x]) atomicAdd(&n_evals[threadIdx.x], s_evals[threadIdx.x]);
 }
 
-static int make_set(const niq_model* const* models, int nfunc, ModelSet& S, int& maxw, int& wfloats, int& maxlayer) {
-    NIQ_REQUIRE(models && nfunc >= 1 && nfunc <= kMaxFuncs, NIQ_ERR_INVALID_ARG, "nfunc must be in [1, %d]", kMaxFuncs);
-    S.n = nfunc;
-    maxw = 0; wfloats = 0; maxlayer = 0;
-    for (int f = 0; f < nfunc; ++f) {
-        NIQ_REQUIRE(models[f], NIQ_ERR_INVALID_ARG, "null model %d", f);
-        S.m[f] = models[f]->ref();
-        S.woff[f] = wfloats;
-        wfloats += models[f]->hdr.n_weight_floats;
-        maxw = maxw > models[f]->hdr.max_width ? maxw : models[f]->hdr.max_width;
-        const int ml = max_layer_floats(models[f]->hdr);
-        maxlayer = maxlayer > ml ? maxlayer : ml;
-    }
-    return NIQ_OK;
-}
-
 __global__ void k_ray_init(float* step, int* live, long long n, float init_step) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         step[i] = init_step;
@@ -251,21 +222,6 @@ static void fill_ray_init(float* step, int* live, long long n, float init_step, 
     long long blocks = (n + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     k_ray_init<<<(int)blocks, 256, 0, s>>>(step, live, n, init_step);
-}
-
-static CastDev to_dev(const niq_cast_opts& c) {
-    CastDev d;
-    d.hit_eps = c.hit_eps;
-    d.max_dist = c.max_dist;
-    d.safety = c.safety_factor;
-    d.grow = c.interval_grow_fac;
-    d.shrink = c.interval_shrink_fac;
-    // src/queries.py:148: ones(N) * interval_init_size * max_dist, in float32
-    volatile float a = 1.0f * c.interval_init_size;
-    d.init_step = a * c.max_dist;
-    d.n_max_step = c.n_max_step;
-    d.n_substeps = c.n_substeps;
-    return d;
 }
 
 }  // namespace niq

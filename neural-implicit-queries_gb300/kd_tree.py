@@ -212,3 +212,55 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
                 if cap > (1 << 31):
                     raise
     return _io.back(dist, kind), _io.back(loc, kind)
+
+
+def _seed(rngkey):
+    """A 64-bit seed from a JAX-style key ((2,) uint32), an int or None."""
+    if rngkey is None:
+        return 0
+    a = np.asarray(rngkey).reshape(-1).astype(np.uint64)
+    v = 0
+    for x in a.tolist():
+        v = ((v * 0x100000001B3) ^ int(x)) & 0xFFFFFFFFFFFFFFFF
+    return v
+
+
+def sample_surface(func, params, lower, upper, n_samples, width, rngkey, n_node_thresh=4096):
+    """src/kd_tree.py:254-292: ``n_samples`` points with |f| < width, drawn uniformly
+    from the unknown nodes of a level-set tree built with offset ``width`` and
+    ``node_terminate_thresh=n_node_thresh``.  Returns an (n_samples, 3) array."""
+    t = _io.require_cuda()
+    ws_t, cap, counts, m = _tree_device(func, params, lower, upper, None, n_node_thresh, 0, width, True)
+    n_nodes = int(counts[0])
+    if n_nodes == 0:
+        raise RuntimeError("the level-set tree has no unknown node within the width")
+    lo, hi = _tree_nodes(ws_t, cap, 0, 0, n_nodes)
+    lo, hi = lo.contiguous(), hi.contiguous()
+    per = min(3 * int(n_samples), 100000)    # src/kd_tree.py:276
+    L = _lib.load()
+    ws_bytes = L.niq_sample_workspace_size(per)
+    ws = _io.workspace(ws_bytes)
+    out = t.empty((int(n_samples), 3), dtype=t.float32, device='cuda')
+    found = _lib.C.c_int64(0)
+    _lib.check(L.niq_sample_surface(m.handle, n_nodes, _io.ptr(lo), _io.ptr(hi), int(n_samples), float(width),
+                                    _seed(rngkey), per, 100000, _io.ptr(out), _lib.C.byref(found), _io.ptr(ws),
+                                    ws_bytes, _io.stream_handle()))
+    return out.cpu().numpy()
+
+
+def bulk_properties(func, params, lower, upper, rngkey, n_expand=int(1e4), n_sample=int(1e6)):
+    """src/kd_tree.py:836-863: ``(mass, centroid)`` of the region f < 0: interior nodes of
+    a level-set tree (``node_terminate_thresh=n_expand``) exactly, its unknown nodes by
+    ``n_sample`` Monte Carlo points."""
+    ws_t, cap, counts, m = _tree_device(func, params, lower, upper, None, n_expand, 1, 0., True)
+    nu, ni = int(counts[0]), int(counts[1])
+    ulo, uhi = _tree_nodes(ws_t, cap, 1, 0, nu)
+    ilo, ihi = _tree_nodes(ws_t, cap, 1, 1, ni)
+    L = _lib.load()
+    ws_bytes = L.niq_sample_workspace_size(int(n_sample))
+    ws = _io.workspace(ws_bytes)
+    res = (_lib.C.c_double * 4)()
+    _lib.check(L.niq_bulk_properties(m.handle, ni, _io.ptr(ilo.contiguous()), _io.ptr(ihi.contiguous()), nu,
+                                     _io.ptr(ulo.contiguous()), _io.ptr(uhi.contiguous()), int(n_sample),
+                                     _seed(rngkey), res, _io.ptr(ws), ws_bytes, _io.stream_handle()))
+    return float(res[0]), np.array([res[1], res[2], res[3]], np.float32)

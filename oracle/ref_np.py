@@ -738,6 +738,68 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts):
     return out_t, out_hit, out_count, n_steps
 
 
+_TET = np.array(((1., -1., -1.), (-1., -1., 1.), (-1., 1., -1.), (1., 1., 1.)), np.float32)
+
+
+def outward_normals(funcs, params_list, hit_pos, hit_ids, eps):
+    """src/render.py:53-90 ('finite_differences'): tetrahedron central differences,
+    normalised, of the function each point hit; zeros where none."""
+    f32 = funcs[0].dtype
+    hit_pos = np.asarray(hit_pos, f32)
+    offsets = (_TET * np.asarray(eps, f32)).astype(f32)
+    out = np.zeros_like(hit_pos)
+    for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
+        pts = (hit_pos[:, None, :] + offsets[None]).reshape(-1, 3).astype(f32)
+        samples = func(params, pts).reshape(-1, 4)
+        grad = np.sum(offsets[None] * samples[:, :, None], axis=1).astype(f32)
+        grad = normalize(grad).astype(f32)
+        out = np.where((hit_ids == fid)[:, None], grad, out)
+    return out
+
+
+def _map_coordinates_linear_nearest(img, x, y):
+    """jax.scipy.ndimage.map_coordinates(img, (x, y), order=1, mode='nearest') for a 2-D
+    image: corner weights (1-w, w) per axis, indices clamped to the image."""
+    x0, y0 = np.floor(x), np.floor(y)
+    wx1, wy1 = (x - x0).astype(np.float32), (y - y0).astype(np.float32)
+    wx0, wy0 = (1 - wx1).astype(np.float32), (1 - wy1).astype(np.float32)
+    xi = [np.clip(x0.astype(np.int64), 0, img.shape[0] - 1), np.clip(x0.astype(np.int64) + 1, 0, img.shape[0] - 1)]
+    yi = [np.clip(y0.astype(np.int64), 0, img.shape[1] - 1), np.clip(y0.astype(np.int64) + 1, 0, img.shape[1] - 1)]
+    acc = np.zeros(x.shape, np.float32)
+    for a, wa in ((0, wx0), (1, wx1)):
+        for b, wb in ((0, wy0), (1, wy1)):
+            acc = (acc + img[xi[a], yi[b]] * (wa * wb)).astype(np.float32)
+    return acc
+
+
+def shade_image(shading, ray_dirs, hit_normals, hit_ids, up_dir, matcaps, colors):
+    """src/render.py:161-224 plus the white background of :139."""
+    f32 = np.float32
+    n = np.asarray(hit_normals, f32)
+    if shading == 'normal':
+        c = ((n + 1.) / 2.).astype(f32)
+    else:
+        d = np.asarray(ray_dirs, f32)
+        r = normalize(d).astype(f32)
+        up = np.asarray(up_dir, f32)
+        ray_up = normalize((up[None] - np.sum(up[None] * r, -1, keepdims=True) * r).astype(f32)).astype(f32)
+        ray_left = np.cross(d, ray_up).astype(f32)
+        u = (np.sum(-ray_left * n, -1) * f32(.98)).astype(f32)
+        v = (np.sum(ray_up * n, -1) * f32(.98)).astype(f32)
+        H, W = matcaps[0].shape[:2]
+        x = ((u + 1.) / 2. * H).astype(f32)
+        y = ((-v + 1.) / 2. * W).astype(f32)
+        cols = np.ones((n.shape[0], 3), f32)
+        for fid, col in enumerate(colors, start=1):
+            cols = np.where((hit_ids == fid)[:, None], np.asarray(col, f32)[None], cols)
+        ck = (1. - (cols[:, 0] + cols[:, 2] + cols[:, 1])).astype(f32)
+        c = np.zeros((n.shape[0], 3), f32)
+        for ch in range(3):
+            m = [_map_coordinates_linear_nearest(np.asarray(mc, f32)[..., ch], x, y) for mc in matcaps]
+            c[:, ch] = cols[:, 0] * m[0] + cols[:, 2] * m[2] + cols[:, 1] * m[1] + ck * m[3]
+    return np.where((hit_ids > 0)[:, None], c, f32(1.)).astype(f32)
+
+
 # ----------------------------------------------------------------------------------------
 # Level-set kd-tree  (src/kd_tree.py:19-218)
 # ----------------------------------------------------------------------------------------
@@ -813,6 +875,45 @@ def construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_ter
 # ----------------------------------------------------------------------------------------
 # Hierarchical marching cubes  (src/kd_tree.py:338-399, src/extract_cell.py:306-421)
 # ----------------------------------------------------------------------------------------
+
+def sample_surface(func, params, lower, upper, n_samples, width, rng, n_node_thresh=4096):
+    """src/kd_tree.py:254-292 with NumPy's generator in place of JAX's: uniform node,
+    uniform point in it, kept when |f| < width, until n_samples are found."""
+    d = construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_terminate_thresh=n_node_thresh,
+                                                offset=width)
+    lo, hi = d['unknown_node_lower'][d['unknown_node_valid']], d['unknown_node_upper'][d['unknown_node_valid']]
+    per = min(3 * n_samples, 100000)
+    found = []
+    total = 0
+    while total < n_samples:
+        idx = rng.integers(0, lo.shape[0], per)
+        p = (lo[idx] + rng.uniform(0, 1, (per, 3)).astype(np.float32) * (hi[idx] - lo[idx])).astype(np.float32)
+        keep = p[np.abs(func(params, p)) < width]
+        found.append(keep)
+        total += keep.shape[0]
+    return np.concatenate(found)[:n_samples], (lo, hi)
+
+
+def bulk_properties(func, params, lower, upper, rng, n_expand=10000, n_sample=1000000):
+    """src/kd_tree.py:836-863 with NumPy's generator: interior nodes exactly, unknown
+    nodes by Monte Carlo; returns (mass, centroid) in float64."""
+    d = construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_terminate_thresh=n_expand,
+                                                with_interior_nodes=True)
+    ilo = d['interior_node_lower'][d['interior_node_valid']].astype(np.float64)
+    ihi = d['interior_node_upper'][d['interior_node_valid']].astype(np.float64)
+    vol = np.prod(ihi - ilo, axis=-1)
+    mass_i = vol.sum()
+    cen_i = (vol[:, None] * 0.5 * (ilo + ihi)).sum(0)
+    lo = d['unknown_node_lower'][d['unknown_node_valid']]
+    hi = d['unknown_node_upper'][d['unknown_node_valid']]
+    idx = rng.integers(0, lo.shape[0], n_sample)
+    p = (lo[idx] + rng.uniform(0, 1, (n_sample, 3)).astype(np.float32) * (hi[idx] - lo[idx])).astype(np.float32)
+    inside = func(params, p) < 0
+    vps = np.prod((hi - lo).astype(np.float64), axis=-1).sum() / n_sample
+    mass = mass_i + vps * inside.sum()
+    cen = (cen_i + vps * p[inside].astype(np.float64).sum(0)) / mass
+    return mass, cen
+
 
 def extract_triangles_from_subcells(func, params, mc_data, n_sub_depth, cell_lo, cell_hi):
     """src/extract_cell.py:366-421 batched over leaves: returns tris (L, S*5, 3, 3) and
