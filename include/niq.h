@@ -99,6 +99,16 @@ typedef struct niq_cast_opts {
 /* ---- library ---------------------------------------------------------------------- */
 const char* niq_last_error(void);
 int niq_version(void);
+/* Launch parameters an autotuner may set for the whole process (0 = the built-in
+ * choice): NIQ_TUNE_BATCHED_CHUNK queries per work chunk of niq_batched_closest_point
+ * (32..4096, default 128); NIQ_TUNE_BATCHED_CTAS_PER_SM and NIQ_TUNE_TREE_CTAS_PER_SM cap
+ * the resident CTAs per SM of those persistent kernels.  No counterpart in the
+ * reference (its batch sizes are arguments, its launches XLA's). */
+#define NIQ_TUNE_BATCHED_CHUNK        0
+#define NIQ_TUNE_BATCHED_CTAS_PER_SM  1
+#define NIQ_TUNE_TREE_CTAS_PER_SM     2
+int niq_tune_set(int32_t param, int32_t value);
+int niq_tune_get(int32_t param, int32_t* value);
 /* Number of SMs and resident-CTA counts of the current device (for workspace sizing). */
 int niq_device_info(int32_t* sm_count, int32_t* max_smem_per_block);
 

@@ -64,6 +64,8 @@ _SIGS = {
     'niq_last_error': (C.c_char_p, []),
     'niq_version': (C.c_int, []),
     'niq_device_info': (C.c_int, [C.POINTER(_I32), C.POINTER(_I32)]),
+    'niq_tune_set': (C.c_int, [_I32, _I32]),
+    'niq_tune_get': (C.c_int, [_I32, C.POINTER(_I32)]),
     'niq_model_create': (C.c_int, [_P, _SZ, C.POINTER(_P)]),
     'niq_model_destroy': (C.c_int, [_P]),
     'niq_model_info': (C.c_int, [_P, C.POINTER(_I32), C.POINTER(_I32)]),

@@ -1,6 +1,7 @@
 // capi.cu -- library-level entry points: errors, device info, model upload.
 #include <cstdarg>
 #include <cmath>
+#include <atomic>
 #include <mutex>
 #include "niq_host.cuh"
 
@@ -19,6 +20,10 @@ int cuda_fail(cudaError_t e, const char* where) {
     set_error("CUDA error %s (%d) in %s", cudaGetErrorString(e), (int)e, where);
     return NIQ_ERR_CUDA;
 }
+
+static std::atomic<int> g_tune[kTuneCount];
+
+int tune_value(int param) { return (param >= 0 && param < kTuneCount) ? g_tune[param].load() : 0; }
 
 static DeviceInfo g_info[64];
 static std::mutex g_info_mu;
@@ -78,6 +83,21 @@ extern "C" {
 const char* niq_last_error(void) { return g_err; }
 
 int niq_version(void) { return 1; }
+
+int niq_tune_set(int32_t param, int32_t value) {
+    NIQ_REQUIRE(param >= 0 && param < kTuneCount, NIQ_ERR_INVALID_ARG, "unknown tuning parameter %d", param);
+    NIQ_REQUIRE(value >= 0, NIQ_ERR_INVALID_ARG, "tuning values are >= 0 (0: built-in choice)");
+    NIQ_REQUIRE(param != kTuneBatchedChunk || value == 0 || (value >= 32 && value <= 4096), NIQ_ERR_INVALID_ARG,
+                "batched chunk must be in [32, 4096]");
+    g_tune[param].store(value);
+    return NIQ_OK;
+}
+
+int niq_tune_get(int32_t param, int32_t* value) {
+    NIQ_REQUIRE(param >= 0 && param < kTuneCount && value, NIQ_ERR_INVALID_ARG, "bad argument");
+    *value = g_tune[param].load();
+    return NIQ_OK;
+}
 
 int niq_device_info(int32_t* sm_count, int32_t* max_smem_per_block) {
     const DeviceInfo& d = device_info();

@@ -11,7 +11,8 @@
 
 namespace niq {
 
-constexpr int kChunk = 128;
+constexpr int kChunk = 128;     // default queries per chunk (tunable: NIQ_TUNE_BATCHED_CHUNK)
+constexpr int kMinChunk = 32;   // smallest tunable chunk: sizes the workspace
 constexpr int kBStack = 96;
 constexpr int kBNT = 256;
 
@@ -278,7 +279,7 @@ size_t slots_max() { return (size_t)device_info().sm_count * 8 * 64; }
 extern "C" {
 
 size_t niq_batched_closest_point_workspace_size(int64_t total_queries, int32_t n_jobs) {
-    const size_t n_chunks = (size_t)(total_queries / kChunk) + (size_t)n_jobs + 1;
+    const size_t n_chunks = (size_t)(total_queries / kMinChunk) + (size_t)n_jobs + 1;
     return al(64) + al(n_chunks * sizeof(BChunk)) + al(n_chunks * 4) + al((size_t)(n_jobs + 1) * sizeof(NiqModelRef)) +
            al(slots_max() * kBStack * 24) + 1024;
 }
@@ -310,15 +311,16 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     // chunks, largest model cost first (longest-processing-time order)
     std::vector<BChunk> chunks;
     std::vector<double> cost;
+    const int chunk_q = tune_value(kTuneBatchedChunk) > 0 ? tune_value(kTuneBatchedChunk) : kChunk;
     for (int j = 0; j < n_jobs; ++j) {
         const NiqSpecHeader& H = models[job_model[j]]->hdr;
         double per_q = 0;
         for (int l = 0; l < H.n_layers; ++l) per_q += (double)H.layers[l].in * H.layers[l].out;
-        for (long long b = 0; b < query_count[j]; b += kChunk) {
+        for (long long b = 0; b < query_count[j]; b += chunk_q) {
             BChunk c;
             c.model = job_model[j];
             c.q_begin = (int)(query_offset[j] + b);
-            c.q_count = (int)std::min<long long>(kChunk, query_count[j] - b);
+            c.q_count = (int)std::min<long long>(chunk_q, query_count[j] - b);
             c.pad = 0;
             chunks.push_back(c);
             cost.push_back(per_q * c.q_count);
@@ -378,7 +380,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
         int rc = prepare_kernel(kern, smem);
         if (rc) return rc;
         int grid = 0;
-        rc = persistent_grid(kern, kBNT, smem, (long long)n_chunks, &grid);
+        rc = persistent_grid(kern, kBNT, smem, (long long)n_chunks, &grid, tune_value(kTuneBatchedCtasPerSm));
         if (rc) return rc;
         NIQ_REQUIRE((size_t)grid * 64 <= slots_max(), NIQ_ERR_UNSUPPORTED, "slot count");
         kern<<<grid, kBNT, smem, s>>>(a, d_tpi);

@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
     const float gam0 = C ? H.layers[0].gamma : 0.f;
     unsigned int epoch = 0;
     if (threadIdx.x == 0) s_boxes = 0;
+    __syncthreads();  // staged weights and the counter visible before warps start on their own
 
     for (int L = level0; L < kTreeMaxLevels; ++L) {
         const long long n_in_raw = (long long)*((volatile unsigned long long*)&ws->level_count[L]);
@@ -86,13 +87,11 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
         const float* in_hi = B.lvl_hi[L & 1];
         float* out_lo = B.lvl_lo[(L + 1) & 1];
         float* out_hi = B.lvl_hi[(L + 1) & 1];
-        while (true) {
-            __syncthreads();
-            if (threadIdx.x == 0) s_base = (long long)atomicAdd(&ws->grab[L], (unsigned long long)ITEMS);
-            __syncthreads();
-            const long long base = s_base;
-            if (base >= n_in) break;
-            const long long nid = base + item;
+        // One tile of nodes starting at nid0: the items of the whole CTA (block mode) or of
+        // this warp only (warp mode: weights resident, warps claim and run independently).
+        auto tile = [&](long long nid0, auto warp_mode) {
+            constexpr bool WM = decltype(warp_mode)::value;
+            const long long nid = nid0 + (WM ? (item % (32 / TPI)) : item);
             const bool valid = nid < n_in;
             // ---- input rows: center and diagonal half extents (src/implicit_function.py:33-37)
             float* xs = st + item * R * LD;
@@ -119,8 +118,9 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
                     }
                 }
             }
-            __syncthreads();
-            tile_forward<Cfg, C>(H, M.w, sW, sw_cap, resident, plan, st, ob);
+            if (WM) __syncwarp();
+            else __syncthreads();
+            tile_forward<Cfg, C, WM>(H, M.w, sW, sw_cap, resident, plan, st, ob);
             // ---- consume: one owner lane per item; every lane joins the warp votes
             int type = -1;
             if (g == 0 && valid) {
@@ -164,6 +164,25 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
                     }
                 }
                 atomicAdd(&s_boxes, 1ull);
+            }
+        };
+        if (resident) {
+            // warp mode: a warp claims 32 / TPI consecutive nodes at a time
+            while (true) {
+                unsigned long long b0 = 0;
+                if ((threadIdx.x & 31) == 0) b0 = atomicAdd(&ws->grab[L], (unsigned long long)(32 / TPI));
+                b0 = __shfl_sync(0xffffffffu, b0, 0);
+                if ((long long)b0 >= n_in) break;
+                tile((long long)b0, std::integral_constant<bool, true>());
+            }
+        } else {
+            while (true) {
+                __syncthreads();
+                if (threadIdx.x == 0) s_base = (long long)atomicAdd(&ws->grab[L], (unsigned long long)ITEMS);
+                __syncthreads();
+                const long long base = s_base;
+                if (base >= n_in) break;
+                tile(base, std::integral_constant<bool, false>());
             }
         }
         if (!COOP) {
@@ -265,6 +284,8 @@ static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float*
         int per_sm = 0;
         NIQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kNT, p.bytes));
         NIQ_REQUIRE(per_sm >= 1, NIQ_ERR_UNSUPPORTED, "tree kernel does not fit on an SM");
+        if (tune_value(kTuneTreeCtasPerSm) > 0 && per_sm > tune_value(kTuneTreeCtasPerSm))
+            per_sm = tune_value(kTuneTreeCtasPerSm);
         const int grid = per_sm * device_info().sm_count;
         NiqModelRef M = m->ref();
         int level0 = 0;
@@ -463,6 +484,8 @@ extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void
         int per_sm = 0;
         NIQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kNT, p.bytes));
         NIQ_REQUIRE(per_sm >= 1, NIQ_ERR_UNSUPPORTED, "tree kernel does not fit on an SM");
+        if (tune_value(kTuneTreeCtasPerSm) > 0 && per_sm > tune_value(kTuneTreeCtasPerSm))
+            per_sm = tune_value(kTuneTreeCtasPerSm);
         const int grid = per_sm * device_info().sm_count;
         int level0 = 0;
         int fixed = p.fixed_floats, swc = p.sw_cap, res = p.resident;

@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 const float* whi = a.tcw + a.tc_off[li];
                 const float* wlo = whi + (long long)chunks * o16 * kTcKC;
                 const uint32_t idesc = tc::idesc_tf32(128, o16);
+                float g_bs = 0.f, g_es = 0.f, g_rho = 0.f;   // column tid of the base, err, rounding rows
                 for (int c = 0; c < chunks; ++c) {
                     const int s = c & 1;
                     if (!wait_stage(s)) { fail = true; }
@@ -274,29 +275,26 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         tc::mma_commit(&bar[s]);
                     }
                     ++n_commit[s];
-                    if (c == 0) {
-                        // base and err rows while the tensor cores work (src/affine_layers.py:11-31)
-                        const float* A = a.M.w + L.a_off;
-                        const float gam = C ? L.gamma : 0.f;
-                        float bs = 0.f, es = 0.f, rho = 0.f;
-                        const int j = tid;
-                        if (j < out) {
-                            for (int k = 0; k < L.in; ++k) {
-                                const float w = __ldg(A + k * L.out_pad + j);
-                                bs = fmaf(s_base[k], w, bs);
-                                es = fmaf(s_err[k], fabsf(w), es);
-                                if (C) rho = __fmaf_ru(s_fold[k], fabsf(w), rho);
-                            }
-                            const float bj = a.M.w[L.b_off + j];
-                            bs = __fadd_rn(bs, bj);
-                            if (C) {
-                                es = __fmul_ru(es, 1.f + 2.f * gam);
-                                rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))),
-                                                (float)(L.in + 2) * NIQ_TINY);
+                    // base, err and rounding rows while the tensor cores work
+                    // (src/affine_layers.py:11-31): column j of the staged weight chunk,
+                    // hi + lo = the fp32 weight exactly, against the chunk's 16 inputs
+                    if (tid < out) {
+                        const float* wh = stg + 2 * kTcRows * kTcKC;
+                        const float* wl = stg + 3 * kTcRows * kTcKC;
+#pragma unroll
+                        for (int q = 0; q < kTcKC / 4; ++q) {
+                            const int off = (int)(tc::kmajor_offset(tid, 4 * q, kTcKC) >> 2);
+                            const float4 h = *reinterpret_cast<const float4*>(wh + off);
+                            const float4 l = *reinterpret_cast<const float4*>(wl + off);
+                            const float w4[4] = {h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w};
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const int k = c * kTcKC + 4 * q + e;
+                                g_bs = fmaf(s_base[k], w4[e], g_bs);
+                                g_es = fmaf(s_err[k], fabsf(w4[e]), g_es);
+                                if (C) g_rho = __fmaf_ru(s_fold[k], fabsf(w4[e]), g_rho);
                             }
                         }
-                        __syncthreads();  // every thread read the old vectors
-                        if (j < NIQ_MAX_WIDTH) { s_base[j] = bs; s_err[j] = es; s_rho[j] = rho; }
                     }
                 }
                 // every MMA of the layer complete before TMEM is read; a wait that gave up
@@ -304,10 +302,25 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 for (int s = 0; s < 2; ++s)
                     if (!wait_stage(s)) fail = true;
                 tc::fence_after_sync();
-                fail = __syncthreads_or(fail ? 1 : 0) != 0;
+                fail = __syncthreads_or(fail ? 1 : 0) != 0;   // also: every thread read the old vectors
                 if (fail) {
                     if (tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
                     break;
+                }
+                if (tid < out) {
+                    const float gam = C ? L.gamma : 0.f;
+                    const float bj = a.M.w[L.b_off + tid];
+                    g_bs = __fadd_rn(g_bs, bj);
+                    if (C) {
+                        g_es = __fmul_ru(g_es, 1.f + 2.f * gam);
+                        g_rho = __fadd_ru(__fmaf_ru(g_rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))),
+                                          (float)(L.in + 2) * NIQ_TINY);
+                    }
+                }
+                if (tid < NIQ_MAX_WIDTH) {
+                    s_base[tid] = tid < out ? g_bs : 0.f;
+                    s_err[tid] = tid < out ? g_es : 0.f;
+                    s_rho[tid] = tid < out ? g_rho : 0.f;
                 }
             }
             // ---------------- activation epilogue (src/affine.py:164-193)

@@ -10,6 +10,9 @@
 namespace niq {
 
 void set_error(const char* fmt, ...);
+// Launch parameters an autotuner may set (niq_tune_set); 0 means the built-in choice.
+enum TuneParam : int { kTuneBatchedChunk = 0, kTuneBatchedCtasPerSm = 1, kTuneTreeCtasPerSm = 2, kTuneCount = 3 };
+int tune_value(int param);
 // Checks a packed spec header against its byte size (capi.cu).
 int validate_spec(const NiqSpecHeader& H, size_t bytes);
 int cuda_fail(cudaError_t e, const char* where);
@@ -84,10 +87,11 @@ inline int prepare_kernel(K kernel, size_t smem) {
 }
 
 template <class K>
-inline int persistent_grid(K kernel, int nt, size_t smem, long long work_tiles, int* grid) {
+inline int persistent_grid(K kernel, int nt, size_t smem, long long work_tiles, int* grid, int max_per_sm = 0) {
     int per_sm = 0;
     NIQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem));
     if (per_sm < 1) { set_error("kernel does not fit on an SM (smem %zu)", smem); return NIQ_ERR_UNSUPPORTED; }
+    if (max_per_sm > 0 && per_sm > max_per_sm) per_sm = max_per_sm;
     long long g = (long long)per_sm * device_info().sm_count;
     if (work_tiles < g) g = work_tiles;
     if (g < 1) g = 1;

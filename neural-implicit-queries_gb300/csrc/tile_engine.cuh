@@ -272,7 +272,9 @@ NIQ_HOST_DEVICE int layer_floats(const NiqLayer& L) { return L.in_pad * L.out_pa
 //        otherwise it must hold at least max_layer_floats floats and each layer is
 //        staged in turn (chunked over k if it does not fit `sw_cap`).
 // ----------------------------------------------------------------------------------
-template <class Cfg, bool C>
+// WARP: the caller's warps work independently (their own items, weights resident): the
+// pass then ends with a warp barrier, and `out` is visible to the item's own warp only.
+template <class Cfg, bool C, bool WARP = false>
 __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ gW, float* __restrict__ sW,
                              int sw_cap, bool resident, const RowPlan plan,
                              float* __restrict__ st, float* __restrict__ out) {
@@ -540,7 +542,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
         }
         // layer output visible before the next layer reads it (the item's own warp), and
         // after the last layer, every item's `out` row visible to the whole block
-        if (last) __syncthreads();
+        if (last && !WARP) __syncthreads();
         else __syncwarp();
     }
 }

@@ -14,6 +14,9 @@ from . import _io, _lib
 from .mlp import device_model
 
 _TREE_CAP0 = 1 << 20
+# node capacity that last sufficed, per (model blob, split depth, threshold, flags, offset):
+# repeated queries start there instead of failing and retrying from the default
+_TREE_CAP_SEEN = {}
 
 
 def _host3(x):
@@ -30,6 +33,8 @@ def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh,
     cap = _TREE_CAP0
     if split_depth is not None:
         cap = max(64, min(cap, 2 ** (split_depth + 1)))
+    key = (m.fingerprint, split_depth, node_terminate_thresh, flags, float(offset), bo.mode, bo.conservative)
+    cap = max(cap, _TREE_CAP_SEEN.get(key, 0))
     fn = L.niq_levelset_tree if persistent else L.niq_levelset_tree_plain
     while True:
         ws_bytes = L.niq_tree_workspace_size(cap, flags)
@@ -40,6 +45,7 @@ def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh,
                           -1 if split_depth is None else int(split_depth),
                           0 if node_terminate_thresh is None else int(node_terminate_thresh), float(offset), flags,
                           cap, _io.ptr(counts), _io.ptr(ws), ws_bytes, _io.stream_handle()))
+            _TREE_CAP_SEEN[key] = cap
             return ws, cap, counts.cpu().numpy(), m
         except _lib.NIQCapacityError:
             del ws

@@ -127,3 +127,18 @@ def test_generate_implicit_modes(niq):
         u.generate_implicit_from_params(p, 'bogus')
     with pytest.raises(ValueError):
         niq.affine.AffineContext('nope')
+
+
+def test_tuning_parameters_roundtrip(niq):
+    """niq_tune_set/get on the host (no device work): values stick, bad ones are refused."""
+    at = niq.autotune
+    old = at.get_params()
+    try:
+        at.set_params(batched_chunk=64, batched_ctas_per_sm=1, tree_ctas_per_sm=2)
+        assert at.get_params() == {'batched_chunk': 64, 'batched_ctas_per_sm': 1, 'tree_ctas_per_sm': 2}
+        with pytest.raises(ValueError):
+            at.set_params(batched_chunk=7)
+        with pytest.raises(ValueError):
+            at.set_params(tree_ctas_per_sm=-1)
+    finally:
+        at.set_params(**old)

@@ -268,3 +268,35 @@ def test_closest_point_persistent_and_batched(niq, R, gpu_ready):
     np.testing.assert_array_equal(out[2][0], d_p[200:])
     d_o, _ = niq.kd_tree.closest_point(f, other, -np.ones(3), np.ones(3), q[100:200], eps=eps, persistent=True)
     np.testing.assert_array_equal(out[1][0], d_o)
+
+
+def test_batched_results_independent_of_tuning(niq, gpu_ready):
+    """The autotuner's parameters change the work split, never a query's result."""
+    models = [niq.workloads.he_mlp([3, w, w, 1], 'relu', seed=30 + i, grid=16) for i, w in enumerate((32, 64, 96))]
+    table = niq.batched.ModelTable(models)
+    f = gf(niq, models[0], conservative=True)
+    rng = np.random.default_rng(9)
+    counts = np.array([70, 300, 45], np.int64)
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    q = rng.uniform(-1.2, 1.2, (int(counts.sum()), 3)).astype(np.float32)
+    lo, hi = -np.ones(3, np.float32), np.ones(3, np.float32)
+    jm = np.arange(3, dtype=np.int32)
+    at = niq.autotune
+    old = at.get_params()
+    try:
+        ref = None
+        for ch, ct in ((128, 0), (32, 1), (512, 0)):
+            at.set_params(batched_chunk=ch, batched_ctas_per_sm=ct)
+            import torch
+            st = torch.zeros(1, dtype=torch.int32, device='cuda')
+            d, l_ = niq.batched.closest_point_packed(f, table, jm, offs, counts, q, lo, hi, 1e-2, status=st,
+                                                     node_budget=4096)
+            d = d.cpu().numpy()
+            if ref is None:
+                ref = d
+            np.testing.assert_array_equal(d, ref)
+        choice, timings = at.tune_batched(f, table, jm, offs, counts, q, lo, hi, 1e-2, node_budget=4096,
+                                          chunks=(32, 128), ctas=(0,), reps=1, use_cache=False)
+        assert choice['batched_chunk'] in (32, 128) and len(timings) == 2
+    finally:
+        at.set_params(**old)
