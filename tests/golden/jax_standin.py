@@ -253,7 +253,11 @@ def _mk_jnp():
         start = np.asarray(start, F32)
         stop = np.asarray(stop, F32)
         s = (np.arange(num, dtype=F32) / F32(num - 1)).astype(F32)
-        return _wrap(start[..., None] * (1 - s) + stop[..., None] * s if start.ndim else start * (1 - s) + stop * s)
+        out = start[..., None] * (1 - s) + stop[..., None] * s if start.ndim else start * (1 - s) + stop * s
+        if dtype is not None and np.issubdtype(np.dtype(dtype), np.integer):
+            # jax computes in floating point and converts (toward zero) to the integer type
+            out = np.trunc(out).astype(np.int32)
+        return _wrap(out)
     m.linspace = linspace
 
     def _f(fn):

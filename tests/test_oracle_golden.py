@@ -135,3 +135,24 @@ def reference_mc_table():
     start = src.index('MC_TRI_TABLE_RAW = [')
     end = src.index(']]', start) + 2
     return np.array(ast.literal_eval(src[start + len('MC_TRI_TABLE_RAW = '):end]))
+
+
+@pytest.mark.parametrize('name', ['one', 'two'])
+def test_cast_rays_frustum(R, name):
+    """The frustum cast restated in oracle/ref_np.py against the reference's own
+    cast_rays_frustum: t, hit id and count on every pixel."""
+    g = golden('frustum.npz')
+    c = g['frustum/cam']
+    cam = (c[0:3], c[3:6], c[6:9], c[9:12], float(c[12]), float(c[13]), int(c[14]), int(c[15]))
+    opts = R.get_default_cast_opts()
+    opts['n_max_step'] = 32
+    opts['n_side_init'] = 2
+    opts['n_substeps'] = 1 if name == 'one' else 2
+    p1 = model_from(g, 'model/relu32x3')
+    ps = (p1,) if name == 'one' else (p1, model_from(g, 'model/relu16'))
+    fs = tuple(R.generate_implicit(p, 'affine_fixed') for p in ps)
+    t, hid, cnt, _ = R.cast_rays_frustum(fs, ps, cam, opts)
+    m = (hid == g[f'frustum/{name}/hit_id']) & (cnt == g[f'frustum/{name}/count']) & \
+        np.isclose(t, g[f'frustum/{name}/t'], rtol=1e-5, atol=1e-6)
+    assert m.mean() >= 0.99, m.mean()
+    assert (g[f'frustum/{name}/hit_id'] > 0).sum() > 0
