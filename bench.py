@@ -49,6 +49,23 @@ def box_flops(params, v=3):
     return 2 * (v + 2) * mlp_macs(params)
 
 
+def max_over_ranks(vals, world):
+    """Each value's maximum over the ranks (all_reduce MAX); identity for one rank."""
+    if world <= 1:
+        return list(vals)
+    import torch
+    import torch.distributed as dist
+    dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    tt = torch.tensor(list(vals), dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return tt.tolist()
+
+
+def replica_rate(units_per_rank, t_max, world):
+    """Whole-job rate of independent replicas: every rank's units over the slowest rank's time."""
+    return world * units_per_rank / t_max
+
+
 def dist_info():
     rank = int(os.environ.get('RANK', '0'))
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -170,6 +187,8 @@ def run_ours(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         return times
 
     tree_t, hmc_t = [], []
@@ -214,11 +233,8 @@ def run_ours(args):
     t_e2e = sum(e2e_times) / len(e2e_times)
 
     # ---- max over ranks
-    if world > 1:
-        tt = torch.tensor([t_step, t_e2e, t_plain], device='cuda')
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step, t_e2e, t_plain = tt.tolist()
-    value = world * n_boxes / t_step
+    t_step, t_e2e, t_plain = max_over_ranks([t_step, t_e2e, t_plain], world)
+    value = replica_rate(n_boxes, t_step, world)
     bf = box_flops(params)
     t_tree = sum(tree_t) / len(tree_t)
     achieved_tf = n_boxes * bf / t_tree / 1e12
@@ -234,10 +250,10 @@ def run_ours(args):
                    "leaves": int(counts_host[0]), "boxes_per_step": n_boxes, "triangles_per_step": n_tris,
                    "mode": "affine_fixed conservative", "l2": "flushed: 256 MiB write between timed steps",
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": world * n_boxes / t_e2e, "unit": "boxes/s", "h2d_bytes_per_step": 24,
+        "e2e": {"value": replica_rate(n_boxes, t_e2e, world), "unit": "boxes/s", "h2d_bytes_per_step": 24,
                 "d2h_bytes_per_step": int(out.nbytes) + 32, "ms_per_step": t_e2e * 1e3,
                 "api": "kd_tree.hierarchical_marching_cubes(depth=8, n_subcell_depth=0)"},
-        "plain": {"value": world * n_boxes / t_plain, "unit": "boxes/s", "ms_per_step": t_plain * 1e3,
+        "plain": {"value": replica_rate(n_boxes, t_plain, world), "unit": "boxes/s", "ms_per_step": t_plain * 1e3,
                   "form": "one launch + host sync per level (niq_levelset_tree_plain)",
                   "persistent_speedup": t_plain / (sum(tree_t) / len(tree_t))},
         "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3},

@@ -11,9 +11,10 @@ arrive from any thread:
   (kd_tree.find_any_intersection)?
 
 A scheduler thread admits queued requests while their estimated device memory fits the
-budget, groups every admitted closest-point request of an admission wave into one
-multi-model launch (batched.closest_point_packed), and issues each group on one of a
-pool of CUDA streams, so work admitted later overlaps work already on the device.  A
+budget, groups the closest-point requests of an admission wave into multi-model
+launches (batched.closest_point_packed) of at most ``closest_group_points`` points,
+smallest first, and issues each launch on one of a pool of CUDA streams, so work
+admitted later overlaps work already on the device.  A
 completion thread polls the streams' events, copies results to the host and resolves
 the request futures; latency is measured from submission to resolution.
 """
@@ -88,6 +89,7 @@ class Server:
         self.upper = np.asarray(upper, np.float32)
         self.budget = int(budget_bytes)
         self.intersect_max_nodes = 1 << 20   # per search level; larger searches fail fast
+        self.closest_group_points = 4096     # closest-point points per multi-model launch
         self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
         # intersections synchronise per search level: they run on their own workers/streams
         self._isect_pool = ThreadPoolExecutor(max_workers=2)
@@ -195,7 +197,23 @@ class Server:
         groups = collections.defaultdict(list)
         for p in cps:
             groups[(float(p.req.eps), int(p.req.node_budget))].append(p)
-        for (eps, budget), grp in groups.items():
+        # split each (eps, budget) group into launches of at most `closest_group_points`
+        # points, smallest requests first, so a small request never waits for the
+        # slowest query of a large one
+        launches = []
+        for key, grp in groups.items():
+            grp = sorted(grp, key=lambda p: len(p.req.points))
+            cur, n = [], 0
+            for p in grp:
+                k = len(p.req.points)
+                if cur and n + k > self.closest_group_points:
+                    launches.append((key, cur))
+                    cur, n = [], 0
+                cur.append(p)
+                n += k
+            if cur:
+                launches.append((key, cur))
+        for (eps, budget), grp in launches:
             # the wave's closest-point requests with one (eps, budget): one multi-model launch
             s = self._next_stream()
             with torch.cuda.stream(s):
