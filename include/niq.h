@@ -273,6 +273,13 @@ int niq_levelset_tree_static(const void* packed_spec_host, const void* packed_sp
                              float* interior_lower, float* interior_upper,
                              float* exterior_lower, float* exterior_upper,
                              int64_t* counts_out, void* stream);
+/* The plain form on the reference's schedule: each level in launches of at most
+ * batch_process_size nodes (one XLA call per batch in src/kd_tree.py:161-172), one host
+ * read of the level size per level.  Same results as niq_levelset_tree_plain. */
+int niq_levelset_tree_batches(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                              const float* upper, int32_t split_depth, int64_t node_terminate_thresh, float offset,
+                              int32_t flags, int64_t batch_process_size, int64_t node_capacity,
+                              int64_t* counts_out, void* workspace, size_t workspace_bytes, void* stream);
 /* Device pointers into a finished tree workspace: kind 0 unknown, 1 interior,
  * 2 exterior; lower/upper are (node_capacity, 3) arrays whose first count rows hold
  * the result. */

@@ -92,6 +92,8 @@ _SIGS = {
     'niq_shade_image': (C.c_int, [_I32, _I64, _P, _P, _P, _PF, _P, _I32, _I32, _PF, _I32, _I32, _P, _P]),
     'niq_levelset_tree_plain': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
                                           _SZ, _P]),
+    'niq_levelset_tree_batches': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _I64,
+                                            _P, _P, _SZ, _P]),
     'niq_tree_result': (C.c_int, [_P, _I64, _I32, _I32, C.POINTER(_P), C.POINTER(_P)]),
     'niq_levelset_tree_static': (C.c_int, [_P, _P, _SZ, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32,
                                            _P, _P, _P, _P, _P, _P, _P, _P]),

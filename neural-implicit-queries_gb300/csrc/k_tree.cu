@@ -44,6 +44,7 @@ struct TreeParams {
     float offset;
     int with_interior, with_exterior;
     int mode_interval;
+    long long batch_start, batch_end;   // node range of the level this launch covers
 };
 
 __device__ __forceinline__ void put_node(float* lo, float* hi, long long i, const float* a, const float* b) {
@@ -83,6 +84,7 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
         }
         const long long n_in = n_in_raw;
         const bool quit = (n_in >= P.thresh) || (L + 1 >= P.n_rounds) || (n_in == 0) || (L + 1 == kTreeMaxLevels);
+        const long long n_lim = n_in < P.batch_end ? n_in : P.batch_end;   // end of this launch's nodes
         const float* in_lo = B.lvl_lo[L & 1];
         const float* in_hi = B.lvl_hi[L & 1];
         float* out_lo = B.lvl_lo[(L + 1) & 1];
@@ -92,7 +94,7 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
         auto tile = [&](long long nid0, auto warp_mode) {
             constexpr bool WM = decltype(warp_mode)::value;
             const long long nid = nid0 + (WM ? (item % (32 / TPI)) : item);
-            const bool valid = nid < n_in;
+            const bool valid = nid < n_lim;
             // ---- input rows: center and diagonal half extents (src/implicit_function.py:33-37)
             float* xs = st + item * R * LD;
             if (g < 4) {
@@ -170,18 +172,20 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
             // warp mode: a warp claims 32 / TPI consecutive nodes at a time
             while (true) {
                 unsigned long long b0 = 0;
-                if ((threadIdx.x & 31) == 0) b0 = atomicAdd(&ws->grab[L], (unsigned long long)(32 / TPI));
+                if ((threadIdx.x & 31) == 0)
+                    b0 = (unsigned long long)P.batch_start + atomicAdd(&ws->grab[L], (unsigned long long)(32 / TPI));
                 b0 = __shfl_sync(0xffffffffu, b0, 0);
-                if ((long long)b0 >= n_in) break;
+                if ((long long)b0 >= n_lim) break;
                 tile((long long)b0, std::integral_constant<bool, true>());
             }
         } else {
             while (true) {
                 __syncthreads();
-                if (threadIdx.x == 0) s_base = (long long)atomicAdd(&ws->grab[L], (unsigned long long)ITEMS);
+                if (threadIdx.x == 0)
+                    s_base = P.batch_start + (long long)atomicAdd(&ws->grab[L], (unsigned long long)ITEMS);
                 __syncthreads();
                 const long long base = s_base;
-                if (base >= n_in) break;
+                if (base >= n_lim) break;
                 tile(base, std::integral_constant<bool, false>());
             }
         }
@@ -244,7 +248,7 @@ __global__ void k_tree_finish(TreeWs* ws, long long* counts) {
 template <bool COOP>
 static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float* lower, const float* upper,
                     int split_depth, long long thresh, float offset, int flags, long long cap, long long* counts,
-                    void* workspace, size_t ws_bytes, cudaStream_t s) {
+                    void* workspace, size_t ws_bytes, cudaStream_t s, long long batch = 0) {
     NIQ_REQUIRE(m && opts && lower && upper && counts, NIQ_ERR_INVALID_ARG, "null argument");
     const int mode = opts->mode;
     NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
@@ -271,6 +275,8 @@ static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float*
     P.with_interior = (flags & NIQ_TREE_WITH_INTERIOR) != 0;
     P.with_exterior = (flags & NIQ_TREE_WITH_EXTERIOR) != 0;
     P.mode_interval = mode == NIQ_MODE_INTERVAL;
+    P.batch_start = 0;
+    P.batch_end = 1ll << 62;
     const bool cons = opts->conservative != 0, slope = mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(m->hdr.max_width);
     int rc = NIQ_OK;
@@ -302,10 +308,20 @@ static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float*
             NIQ_CUDA(cudaStreamSynchronize(s));
             const long long n_in = (long long)cnt[0];
             const bool quit = (n_in >= P.thresh) || (L + 1 >= P.n_rounds) || (n_in == 0) || (L + 1 == kTreeMaxLevels);
-            long long tiles = (n_in + items - 1) / items;
-            int g = (int)(tiles < grid ? (tiles < 1 ? 1 : tiles) : grid);
-            kern<<<g, kNT, p.bytes, s>>>(M, P, ws, B, L, fixed, cap_, res);
-            NIQ_CUDA(cudaGetLastError());
+            // whole level per launch, or the reference's schedule: one launch per batch of
+            // `batch` nodes (src/kd_tree.py:161-172)
+            const long long step = batch > 0 ? batch : (n_in > 0 ? n_in : 1);
+            for (long long b0 = 0; b0 < (n_in > 0 ? n_in : 1); b0 += step) {
+                TreeParams Pb = P;
+                Pb.batch_start = b0;
+                Pb.batch_end = b0 + step;
+                if (b0 > 0) NIQ_CUDA(cudaMemsetAsync(&ws->grab[L], 0, sizeof(unsigned long long), s));
+                const long long nb = (n_in - b0 < step ? n_in - b0 : step);
+                long long tiles = (nb + items - 1) / items;
+                int g = (int)(tiles < grid ? (tiles < 1 ? 1 : tiles) : grid);
+                kern<<<g, kNT, p.bytes, s>>>(M, Pb, ws, B, L, fixed, cap_, res);
+                NIQ_CUDA(cudaGetLastError());
+            }
             if (quit) break;
         }
         return NIQ_OK;
@@ -347,6 +363,16 @@ int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts, 
                             size_t workspace_bytes, void* stream) {
     return run_tree<false>(model, opts, lower, upper, split_depth, node_terminate_thresh, offset, flags, node_capacity,
                            reinterpret_cast<long long*>(counts_out), workspace, workspace_bytes, as_stream(stream));
+}
+
+int niq_levelset_tree_batches(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                              const float* upper, int32_t split_depth, int64_t node_terminate_thresh, float offset,
+                              int32_t flags, int64_t batch_process_size, int64_t node_capacity, int64_t* counts_out,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+    NIQ_REQUIRE(batch_process_size >= 1, NIQ_ERR_INVALID_ARG, "batch_process_size must be >= 1");
+    return run_tree<false>(model, opts, lower, upper, split_depth, node_terminate_thresh, offset, flags, node_capacity,
+                           reinterpret_cast<long long*>(counts_out), workspace, workspace_bytes, as_stream(stream),
+                           batch_process_size);
 }
 
 int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32_t kind, float** lower, float** upper) {
@@ -469,6 +495,8 @@ extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void
     P.with_interior = (flags & NIQ_TREE_WITH_INTERIOR) != 0;
     P.with_exterior = (flags & NIQ_TREE_WITH_EXTERIOR) != 0;
     P.mode_interval = mode == NIQ_MODE_INTERVAL;
+    P.batch_start = 0;
+    P.batch_end = 1ll << 62;
     NiqModelRef M;
     M.hdr = reinterpret_cast<const NiqSpecHeader*>(packed_spec_device);
     M.w = reinterpret_cast<const float*>(reinterpret_cast<const char*>(packed_spec_device) + sizeof(NiqSpecHeader));

@@ -24,8 +24,11 @@ def _host3(x):
     return (_lib.C.c_float * 3)(*a.tolist())
 
 
-def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh, flags, offset, persistent):
-    """Runs the tree on the device; returns (workspace tensor, capacity, counts, model)."""
+def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh, flags, offset, persistent,
+                 batch_process_size=2048):
+    """Runs the tree on the device; returns (workspace tensor, capacity, counts, model).
+    ``persistent``: True (one cooperative launch), False (one launch per level) or
+    'batches' (the reference's schedule: launches of ``batch_process_size`` nodes)."""
     t = _io.require_cuda()
     m = device_model(params)
     bo = func.bound_opts()
@@ -35,7 +38,13 @@ def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh,
         cap = max(64, min(cap, 2 ** (split_depth + 1)))
     key = (m.fingerprint, split_depth, node_terminate_thresh, flags, float(offset), bo.mode, bo.conservative)
     cap = max(cap, _TREE_CAP_SEEN.get(key, 0))
-    fn = L.niq_levelset_tree if persistent else L.niq_levelset_tree_plain
+    if persistent == 'batches':
+        B = int(batch_process_size)
+
+        def fn(*a):
+            return L.niq_levelset_tree_batches(*a[:8], B, *a[8:])
+    else:
+        fn = L.niq_levelset_tree if persistent else L.niq_levelset_tree_plain
     while True:
         ws_bytes = L.niq_tree_workspace_size(cap, flags)
         ws = t.empty(ws_bytes, dtype=t.uint8, device='cuda')
@@ -72,13 +81,14 @@ def construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_ter
                                             compress_after=False, with_childern=False, with_interior_nodes=False,
                                             with_exterior_nodes=False, offset=0., batch_process_size=2048,
                                             persistent=True):
-    """src/kd_tree.py:103-218.  ``batch_process_size`` is accepted for compatibility;
-    the device kernels batch by themselves.  Adds key ``n_boxes_classified``."""
+    """src/kd_tree.py:103-218.  Adds key ``n_boxes_classified``.  ``persistent``: True
+    runs every level in one cooperative launch; False one launch per level; 'batches'
+    the reference's own schedule, one launch per ``batch_process_size`` nodes."""
     if node_terminate_thresh is None and split_depth is None:
         raise ValueError("must specify at least one of node_terminate_thresh or split_depth as a terminating condition")
     flags = (1 if with_interior_nodes else 0) | (2 if with_exterior_nodes else 0)
     ws, cap, counts, _ = _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh, flags, offset,
-                                      persistent)
+                                      persistent, batch_process_size)
     out = {'n_boxes_classified': int(counts[3])}
     for kind, name, on in ((0, 'unknown', True), (1, 'interior', with_interior_nodes),
                            (2, 'exterior', with_exterior_nodes)):

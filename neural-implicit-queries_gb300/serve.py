@@ -29,7 +29,7 @@ from concurrent.futures import Future, ThreadPoolExecutor
 
 import numpy as np
 
-from . import _io, _lib, batched, kd_tree, queries
+from . import _io, _lib, autotune, batched, kd_tree, queries
 from .implicit_mlp_utils import generate_implicit_from_params
 from .mlp import device_model, prepend_op, spatial_transformation
 
@@ -90,7 +90,16 @@ class Server:
         self.budget = int(budget_bytes)
         self.intersect_max_nodes = 1 << 20   # per search level; larger searches fail fast
         self.closest_group_points = 4096     # closest-point points per multi-model launch
-        self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
+        # ray tiles and closest-point launches on separate stream pools, so a light ray
+        # tile never queues behind a heavy closest-point launch on the same stream
+        self.streams = {'rays': [torch.cuda.Stream() for _ in range(max(1, n_streams // 2))],
+                        'closest': [torch.cuda.Stream() for _ in range(max(1, n_streams - n_streams // 2))]}
+        self._rr_kind = {'rays': 0, 'closest': 0}
+        # one closest-point CTA per SM leaves room on every SM for the ray kernels'
+        # CTAs (the persistent launch would otherwise hold the whole GPU); this sets the
+        # process-wide launch parameter (restored by close())
+        self._saved_tuning = autotune.get_params()
+        autotune.set_params(batched_ctas_per_sm=1)
         # intersections synchronise per search level: they run on their own workers/streams
         self._isect_pool = ThreadPoolExecutor(max_workers=2)
         self._isect_streams = [torch.cuda.Stream() for _ in range(2)]
@@ -125,6 +134,7 @@ class Server:
         self._sched.join()
         self._done.join()
         self._isect_pool.shutdown(wait=True)
+        autotune.set_params(**self._saved_tuning)
 
     def stats(self):
         lat = np.array(self.latencies) * 1e3
@@ -138,9 +148,10 @@ class Server:
                 "closest_budget_exhausted": self.budget_exhausted, "by_kind": per_kind}
 
     # ------------------------------------------------------------------ scheduler
-    def _next_stream(self):
-        s = self.streams[self._rr % len(self.streams)]
-        self._rr += 1
+    def _next_stream(self, kind):
+        pool = self.streams[kind]
+        s = pool[self._rr_kind[kind] % len(pool)]
+        self._rr_kind[kind] += 1
         return s
 
     def _schedule(self):
@@ -194,6 +205,17 @@ class Server:
         cps = [p for p in wave if isinstance(p.req, ClosestRequest)]
         rays = [p for p in wave if isinstance(p.req, RayRequest)]
         isects = [p for p in wave if isinstance(p.req, IntersectRequest)]
+        # ray tiles first: they are light and their streams are their own
+        for p in rays:
+            s = self._next_stream('rays')
+            with torch.cuda.stream(s):
+                opts = p.req.opts or queries.get_default_cast_opts()
+                out = queries.cast_rays((self.func,), (self.table.models[p.req.model],),
+                                        np.asarray(p.req.roots, np.float32), np.asarray(p.req.dirs, np.float32),
+                                        opts, return_device=True)
+                ev = torch.cuda.Event()
+                ev.record(s)
+            self._push(('rays', [p], out[:3], ev))
         groups = collections.defaultdict(list)
         for p in cps:
             groups[(float(p.req.eps), int(p.req.node_budget))].append(p)
@@ -215,7 +237,7 @@ class Server:
                 launches.append((key, cur))
         for (eps, budget), grp in launches:
             # the wave's closest-point requests with one (eps, budget): one multi-model launch
-            s = self._next_stream()
+            s = self._next_stream('closest')
             with torch.cuda.stream(s):
                 counts = np.array([len(p.req.points) for p in grp], np.int64)
                 offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
@@ -227,16 +249,6 @@ class Server:
                 ev = torch.cuda.Event()
                 ev.record(s)
             self._push(('closest', grp, (dist, loc, offs, counts, status), ev))
-        for p in rays:
-            s = self._next_stream()
-            with torch.cuda.stream(s):
-                opts = p.req.opts or queries.get_default_cast_opts()
-                out = queries.cast_rays((self.func,), (self.table.models[p.req.model],),
-                                        np.asarray(p.req.roots, np.float32), np.asarray(p.req.dirs, np.float32),
-                                        opts, return_device=True)
-                ev = torch.cuda.Event()
-                ev.record(s)
-            self._push(('rays', [p], out[:3], ev))
         for p in isects:
             s = self._isect_streams[self._isect_rr % len(self._isect_streams)]
             self._isect_rr += 1

@@ -300,3 +300,20 @@ def test_batched_results_independent_of_tuning(niq, gpu_ready):
         assert choice['batched_chunk'] in (32, 128) and len(timings) == 2
     finally:
         at.set_params(**old)
+
+
+@pytest.mark.parametrize('B', [2048, 100])
+def test_tree_schedules_agree(niq, gpu_ready, B):
+    """The persistent tree, one launch per level, and the reference's schedule (launches
+    of batch_process_size nodes) produce the same node sets."""
+    params = niq.workloads.spheres_sdf_model()
+    f = gf(niq, params, conservative=True)
+    sets = []
+    for persistent in (True, False, 'batches'):
+        d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=15,
+                                                                with_interior_nodes=True, batch_process_size=B,
+                                                                persistent=persistent)
+        sets.append({k: {tuple(r) for r in np.concatenate([d[f'{k}_node_lower'], d[f'{k}_node_upper']], 1).tolist()}
+                     for k in ('unknown', 'interior')})
+        assert d['n_boxes_classified'] > 0
+    assert sets[0] == sets[1] == sets[2]

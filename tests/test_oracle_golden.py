@@ -156,3 +156,19 @@ def test_cast_rays_frustum(R, name):
         np.isclose(t, g[f'frustum/{name}/t'], rtol=1e-5, atol=1e-6)
     assert m.mean() >= 0.99, m.mean()
     assert (g[f'frustum/{name}/hit_id'] > 0).sum() > 0
+
+
+def test_c_restatement_matches_numpy_oracle(R):
+    """oracle/cpu_tree.c (the CPU baseline) builds the same leaf set, in the same order,
+    as the NumPy oracle."""
+    from oracle import cpu_tree
+    import importlib
+    niq = importlib.import_module('neural-implicit-queries_gb300')
+    params = niq.workloads.spheres_sdf_model()
+    n, nb, leaves = cpu_tree.levelset_tree(niq.mlp.spec_layers(params), -np.ones(3), np.ones(3), 12,
+                                           want_leaves=True)
+    d = R.construct_uniform_unknown_levelset_tree(R.generate_implicit(params, 'affine_fixed'), params,
+                                                  -np.ones(3), np.ones(3), split_depth=12)
+    ref = np.concatenate([d['unknown_node_lower'], d['unknown_node_upper']], 1)
+    assert n == ref.shape[0] and nb == d['n_boxes_classified']
+    np.testing.assert_array_equal(leaves, ref)
