@@ -165,14 +165,18 @@ def run_ours(args):
                      io.ptr(ws), ws_bytes, stream.cuda_stream))
 
     def hmc_step():
+        # marching cubes on the leaves (n_subcell_depth 0): shared lattice corners once
         n_leaves = int(counts_host[0])
         lo, hi = kd._tree_nodes(ws, cap, 0, 0, n_leaves)
-        lib.check(L.niq_hmc_extract(model.handle, n_leaves, io.ptr(lo), io.ptr(hi), 0, io.ptr(tris), tri_cap,
-                                    io.ptr(ntri), io.ptr(hws), hws.numel(), stream.cuda_stream))
+        lib.check(L.niq_hmc_extract_lattice(model.handle, n_leaves, io.ptr(lo), io.ptr(hi), lo3, hi3, args.split_depth,
+                                            io.ptr(tris), tri_cap, io.ptr(ntri), io.ptr(lws), lws.numel(),
+                                            stream.cuda_stream))
 
     tree_step()
     counts_host = counts.cpu().numpy()
     n_boxes = int(counts_host[3])
+    lws = torch.empty(L.niq_hmc_lattice_workspace_size(lo3, hi3, args.split_depth, int(counts_host[0])),
+                      dtype=torch.uint8, device='cuda')
     hmc_step()
     n_tris = int(ntri.item())
 
@@ -272,7 +276,13 @@ def run_ours(args):
         "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3},
         "roofline": {"bound": "fp32", "kernel": "k_tree (persistent level-set tree)",
                      "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak, "traffic": None,
+                     "frac": achieved_tf / fp32_peak,
+                     # DRAM bytes of one k_tree launch: the ncu capture of the 18-bisection tree
+                     # (profiles/k_tree_k_hmc_spheres64_split18_full.md: 0.444 MB read + 0.191 MB
+                     # written for 332,953 boxes) scaled by boxes to this launch
+                     "traffic": (444160 + 190976) / 332953 * n_boxes,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the "
+                                       "18-bisection tree, scaled to this launch's boxes; the level arrays stay in L2",
                      "flops_per_box": bf,
                      "peak_source": (f"FP32 FMA pipe: {props.multi_processor_count} SMs x 128 lanes x 2 FLOP x "
                                      f"{sm_max:.0f} MHz (MEASURED_PEAKS.json sm_max_mhz); the file has no FP32 "
@@ -573,8 +583,9 @@ def run_batched(args):
 
 def make_serving_requests(niq, n, rng, max_res=512, max_points=16384):
     """The serving mix: ray tiles (64^2..max_res^2 from a random camera at distance 3),
-    closest-point batches (1..max_points points, log-uniform, eps 1e-2, at most 1024
-    nodes per query: the models are untrained, their bounds loose) and pairwise
+    closest-point batches (1..max_points points, log-uniform, eps 1e-2, at most 128
+    nodes per query: the models are untrained, their bounds loose, and a served answer
+    within its node budget is an upper bound) and pairwise
     intersection tests under a random rigid transform (eps 2e-2): 45% / 45% / 10%."""
     srv = niq.serve
     reqs = []
@@ -594,7 +605,7 @@ def make_serving_requests(niq, n, rng, max_res=512, max_points=16384):
         elif u < 0.9:
             k = int(np.exp(rng.uniform(0, np.log(max_points))))
             reqs.append(srv.ClosestRequest(m, rng.uniform(-1.2, 1.2, (k, 3)).astype(np.float32), eps=1e-2,
-                                           node_budget=1024))
+                                           node_budget=128))
         else:
             R = niq.workloads.random_rotation(rng)
             reqs.append(srv.IntersectRequest(m, int(rng.integers(64)), R,

@@ -300,6 +300,18 @@ int niq_hmc_extract(const niq_model* model, int64_t n_leaves, const float* leaf_
  * Same polygons and orientation as src/extract_cell.py:12-268 for every case; pure
  * host code, no device needed. */
 int niq_mc_table(int32_t* out);
+/* The n_subcell_depth = 0 extraction for the leaves of a uniform tree of split_depth
+ * bisections of [root_lower, root_upper]: corners shared by neighbouring leaves are
+ * evaluated once (the leaves are cells of one lattice; a split plane is the same float
+ * in both children), then every leaf is polygonised as niq_hmc_extract does, with the
+ * same arithmetic and the same triangles (in another order).  workspace:
+ * niq_hmc_lattice_workspace_size() bytes. */
+size_t niq_hmc_lattice_workspace_size(const float* root_lower, const float* root_upper, int32_t split_depth,
+                                      int64_t n_leaves);
+int niq_hmc_extract_lattice(const niq_model* model, int64_t n_leaves, const float* leaf_lower,
+                            const float* leaf_upper, const float* root_lower, const float* root_upper,
+                            int32_t split_depth, float* tris_out, int64_t tri_capacity, int64_t* n_tris_out,
+                            void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- pairwise intersection: find_any_intersection (src/kd_tree.py:402-655) ---------- *
  * found_out (device int32[1]) = 1 when an intersection is found, loc_out (device

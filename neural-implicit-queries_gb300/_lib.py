@@ -100,6 +100,8 @@ _SIGS = {
     'niq_hmc_workspace_size': (_SZ, []),
     'niq_hmc_extract': (C.c_int, [_P, _I64, _P, _P, _I32, _P, _I64, _P, _P, _SZ, _P]),
     'niq_mc_table': (C.c_int, [C.POINTER(_I32)]),
+    'niq_hmc_lattice_workspace_size': (_SZ, [_PF, _PF, _I32, _I64]),
+    'niq_hmc_extract_lattice': (C.c_int, [_P, _I64, _P, _P, _PF, _PF, _I32, _P, _I64, _P, _P, _SZ, _P]),
     'niq_intersect_workspace_size': (_SZ, [_P, _P, C.POINTER(BoundOpts), _I64]),
     'niq_find_any_intersection': (C.c_int, [_P, _P, C.POINTER(BoundOpts), _PF, _PF, _F32, _I64, _P, _P, _P, _P, _SZ,
                                             _P]),

@@ -272,6 +272,117 @@ __global__ void __launch_bounds__(kNT) k_hmc(NiqModelRef M, HmcArgs a, unsigned 
     }
 }
 
+// ---------------------------------------------------------------------------------
+// Shared corners (n_subcell_depth = 0 on a uniform tree).  The leaves of a uniform tree
+// are cells of one lattice, and neighbouring leaves share their corner points exactly
+// (a split plane is one float for both children), so each lattice vertex is evaluated
+// once instead of once per leaf touching it.  k_lattice_mark gives every distinct corner
+// a slot (the first leaf to reach it stores its coordinates), the point kernel evaluates
+// the slots, and k_lattice_cells polygonises each leaf from its corners' slots with the
+// same arithmetic as k_hmc.
+// ---------------------------------------------------------------------------------
+struct Lattice {
+    float L[3], h[3];   // lower corner of the root, cell size
+    int n[3];           // vertices per axis (cells + 1)
+};
+
+__device__ __forceinline__ long long lattice_index(const Lattice& G, const float* p) {
+    long long idx = 0;
+    for (int k = 0; k < 3; ++k) {
+        int i = (int)rintf((p[k] - G.L[k]) / G.h[k]);
+        i = min(max(i, 0), G.n[k] - 1);
+        idx = idx * G.n[k] + i;
+    }
+    return idx;
+}
+
+__global__ void k_lattice_mark(long long n_leaves, const float* __restrict__ lo, const float* __restrict__ hi, Lattice G,
+                               int* __restrict__ slot, unsigned long long* __restrict__ n_unique, float* __restrict__ pts,
+                               long long cap, int* err) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 8 * n_leaves;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long l = t >> 3;
+        const int c = (int)(t & 7);
+        float p[3];
+        for (int k = 0; k < 3; ++k) p[k] = c_vert[c][k] ? hi[3 * l + k] : lo[3 * l + k];
+        const long long idx = lattice_index(G, p);
+        if (atomicCAS(&slot[idx], -1, -2) == -1) {
+            const unsigned long long pos = atomicAdd(n_unique, 1ull);
+            if ((long long)pos < cap) {
+                for (int k = 0; k < 3; ++k) pts[3 * pos + k] = p[k];
+                slot[idx] = (int)pos;
+            } else {
+                niq_flag_error(err, NIQ_ERR_CAPACITY);
+            }
+        }
+    }
+}
+
+__global__ void k_lattice_cells(long long n_leaves, const float* __restrict__ blo, const float* __restrict__ bhi,
+                                Lattice G, const int* __restrict__ slot, const float* __restrict__ vals,
+                                float* __restrict__ tris, long long cap, unsigned long long* counter, int* err) {
+    for (long long l0 = blockIdx.x * (long long)blockDim.x; l0 < n_leaves; l0 += (long long)gridDim.x * blockDim.x) {
+        const long long l = l0 + threadIdx.x;
+        const bool valid = l < n_leaves;
+        int n_tri = 0;
+        float ep[12][3];
+        signed char row[16];
+        if (valid) {
+            // the leaf is the only subcell: lower + {0, (upper - lower) / 1} as in k_hmc
+            float lo[3], hi[3];
+            for (int k = 0; k < 3; ++k) {
+                const float delta = __fdiv_rn(__fsub_rn(bhi[3 * l + k], blo[3 * l + k]), 1.f);
+                lo[k] = __fadd_rn(blo[3 * l + k], __fmul_rn(0.f, delta));
+                hi[k] = __fadd_rn(lo[k], delta);
+            }
+            float vv[8];
+            int cs = 0;
+            for (int i = 0; i < 8; ++i) {
+                float p[3];
+                for (int k = 0; k < 3; ++k) p[k] = c_vert[i][k] ? bhi[3 * l + k] : blo[3 * l + k];
+                const int sl = slot[lattice_index(G, p)];
+                vv[i] = sl >= 0 ? vals[sl] : __int_as_float(0x7fffffff);   // every corner was marked
+                cs |= (vv[i] < 0.f) << i;
+            }
+            for (int e = 0; e < 12; ++e) {
+                const int ia = c_edge[e][0], ib = c_edge[e][1];
+                float t = __fdiv_rn(-vv[ia], __fsub_rn(vv[ib], vv[ia]));
+                if (t != t) t = 0.f;
+                t = fminf(fmaxf(t, 0.f), 1.f);
+                for (int k = 0; k < 3; ++k) {
+                    const float pa = c_vert[ia][k] ? hi[k] : lo[k];
+                    const float pb = c_vert[ib][k] ? hi[k] : lo[k];
+                    ep[e][k] = __fadd_rn(__fmul_rn(__fsub_rn(1.f, t), pa), __fmul_rn(t, pb));
+                }
+            }
+            for (int i = 0; i < 16; ++i) row[i] = c_tri[cs][i];
+            for (int tI = 0; tI < 5; ++tI) n_tri += row[3 * tI] != -1;
+        }
+        int incl = n_tri;
+        const int lane = threadIdx.x & 31;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += y;
+        }
+        const int wsum = __shfl_sync(0xffffffffu, incl, 31);
+        unsigned long long wbase = 0;
+        if (lane == 31 && wsum > 0) wbase = atomicAdd(counter, (unsigned long long)wsum);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        long long pos = (long long)wbase + (incl - n_tri);
+        for (int tI = 0, w = 0; tI < 5 && w < n_tri; ++tI) {
+            if (row[3 * tI] == -1) continue;
+            if (pos + w < cap) {
+                float* dst = tris + 9 * (pos + w);
+                for (int vI = 0; vI < 3; ++vI)
+                    for (int k = 0; k < 3; ++k) dst[3 * vI + k] = ep[row[3 * tI + vI]][k];
+            } else {
+                niq_flag_error(err, NIQ_ERR_CAPACITY);
+            }
+            ++w;
+        }
+    }
+}
+
 }  // namespace niq
 
 using namespace niq;
@@ -287,6 +398,89 @@ int niq_mc_table(int32_t* out) {
 }
 
 size_t niq_hmc_workspace_size(void) { return 512; }
+
+// The uniform tree's lattice: simulate split_depth bisections of the root (first longest
+// axis, midpoint, float32 as the tree kernel does) to get the cell size per axis.
+static int lattice_of(const float* root_lower, const float* root_upper, int split_depth, Lattice& G) {
+    float lo[3] = {root_lower[0], root_lower[1], root_lower[2]}, hi[3] = {root_upper[0], root_upper[1], root_upper[2]};
+    int splits[3] = {0, 0, 0};
+    for (int s = 0; s < split_depth; ++s) {
+        const float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+        int d = 0;
+        float em = e0;
+        if (e1 > em) { d = 1; em = e1; }
+        if (e2 > em) d = 2;
+        hi[d] = 0.5f * (lo[d] + hi[d]);
+        ++splits[d];
+    }
+    for (int k = 0; k < 3; ++k) {
+        NIQ_REQUIRE(splits[k] < 24, NIQ_ERR_UNSUPPORTED, "lattice too fine");
+        G.L[k] = root_lower[k];
+        G.h[k] = hi[k] - lo[k];
+        G.n[k] = (1 << splits[k]) + 1;
+    }
+    return NIQ_OK;
+}
+
+size_t niq_hmc_lattice_workspace_size(const float* root_lower, const float* root_upper, int32_t split_depth,
+                                      int64_t n_leaves) {
+    Lattice G;
+    if (!root_lower || !root_upper || lattice_of(root_lower, root_upper, split_depth, G)) return 0;
+    const size_t nv = (size_t)G.n[0] * G.n[1] * G.n[2];
+    const size_t nu = (size_t)(8 * (n_leaves > 0 ? n_leaves : 0));   // distinct corners, at most 8 per leaf
+    return 512 + ((nv * 4 + 255) & ~size_t(255)) + ((nu * 12 + 255) & ~size_t(255)) + ((nu * 4 + 255) & ~size_t(255));
+}
+
+int niq_hmc_extract_lattice(const niq_model* model, int64_t n_leaves, const float* leaf_lower, const float* leaf_upper,
+                            const float* root_lower, const float* root_upper, int32_t split_depth, float* tris_out,
+                            int64_t tri_capacity, int64_t* n_tris_out, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+    NIQ_REQUIRE(model && n_tris_out && root_lower && root_upper && n_leaves >= 0 && tri_capacity >= 0,
+                NIQ_ERR_INVALID_ARG, "bad argument");
+    NIQ_REQUIRE(n_leaves == 0 || (leaf_lower && leaf_upper), NIQ_ERR_INVALID_ARG, "null leaf arrays");
+    NIQ_REQUIRE(tri_capacity == 0 || tris_out, NIQ_ERR_INVALID_ARG, "null triangle array");
+    Lattice G;
+    int rc = lattice_of(root_lower, root_upper, split_depth, G);
+    if (rc) return rc;
+    const size_t need = niq_hmc_lattice_workspace_size(root_lower, root_upper, split_depth, n_leaves);
+    NIQ_REQUIRE(workspace && workspace_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", need);
+    cudaStream_t s = as_stream(stream);
+    rc = ensure_table();
+    if (rc) return rc;
+    NIQ_CUDA(cudaMemsetAsync(n_tris_out, 0, sizeof(int64_t), s));
+    if (n_leaves == 0) return NIQ_OK;
+    char* b = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    unsigned long long* n_unique = reinterpret_cast<unsigned long long*>(b);
+    int* err = reinterpret_cast<int*>(b + 8);
+    const size_t nv = (size_t)G.n[0] * G.n[1] * G.n[2];
+    const long long nu_cap = 8 * n_leaves;
+    int* slot = reinterpret_cast<int*>(b + 256);
+    float* pts = reinterpret_cast<float*>(b + 256 + ((nv * 4 + 255) & ~size_t(255)));
+    float* vals = pts + (((size_t)nu_cap * 12 + 255) & ~size_t(255)) / 4;
+    NIQ_CUDA(cudaMemsetAsync(b, 0, 16, s));
+    NIQ_CUDA(cudaMemsetAsync(slot, 0xFF, nv * 4, s));   // -1: not yet claimed
+    const int grid = (int)std::min<long long>((8 * n_leaves + 255) / 256, 8 * 1024);
+    k_lattice_mark<<<grid, 256, 0, s>>>(n_leaves, leaf_lower, leaf_upper, G, slot, n_unique, pts, nu_cap, err);
+    NIQ_CUDA(cudaGetLastError());
+    unsigned long long nu = 0;
+    NIQ_CUDA(cudaMemcpyAsync(&nu, n_unique, 8, cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    NIQ_REQUIRE((long long)nu <= nu_cap, NIQ_ERR_CAPACITY, "distinct corners overflow");
+    rc = niq_eval_points(model, (int64_t)nu, pts, vals, stream);
+    if (rc) return rc;
+    const int grid2 = (int)std::min<long long>((n_leaves + 255) / 256, 8 * 1024);
+    k_lattice_cells<<<grid2, 256, 0, s>>>(n_leaves, leaf_lower, leaf_upper, G, slot, vals, tris_out, tri_capacity,
+                                          reinterpret_cast<unsigned long long*>(n_tris_out), err);
+    NIQ_CUDA(cudaGetLastError());
+    long long n = 0;
+    int e = 0;
+    NIQ_CUDA(cudaMemcpyAsync(&n, n_tris_out, 8, cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    NIQ_REQUIRE(n <= tri_capacity, NIQ_ERR_CAPACITY, "%lld triangles exceed the capacity %lld", n, (long long)tri_capacity);
+    NIQ_REQUIRE(e == 0, e, "lattice extraction error %d", e);
+    return NIQ_OK;
+}
 
 int niq_hmc_extract(const niq_model* model, int64_t n_leaves, const float* leaf_lower, const float* leaf_upper,
                     int32_t n_subcell_depth, float* tris_out, int64_t tri_capacity, int64_t* n_tris_out,

@@ -424,13 +424,12 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             if (j < out) {
                 const int rk = s_rank[nrows + j];
                 if (rk < keep) {
+                    const float dh = tc::tf32_hi(delta), dl = delta - dh;
                     for (int k = 0; k < o16; k += 4) {
-                        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-                        if (j >= k && j < k + 4) {
-                            const float dh = tc::tf32_hi(delta), dl = delta - dh;
-                            (&h.x)[j - k] = dh;
-                            (&l.x)[j - k] = dl;
-                        }
+                        const float4 h = make_float4(j == k ? dh : 0.f, j == k + 1 ? dh : 0.f, j == k + 2 ? dh : 0.f,
+                                                     j == k + 3 ? dh : 0.f);
+                        const float4 l = make_float4(j == k ? dl : 0.f, j == k + 1 ? dl : 0.f, j == k + 2 ? dl : 0.f,
+                                                     j == k + 3 ? dl : 0.f);
                         const int xi = x_index(rk, k);
                         *reinterpret_cast<float4*>(xs_hi + xi) = h;
                         *reinterpret_cast<float4*>(xs_lo + xi) = l;

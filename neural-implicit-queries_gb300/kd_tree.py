@@ -103,10 +103,12 @@ def construct_uniform_unknown_levelset_tree(func, params, lower, upper, node_ter
 
 
 def hierarchical_marching_cubes(func, params, lower, upper, depth, n_subcell_depth=2,
-                                extract_batch_max_tri_out=1000000, persistent=True):
+                                extract_batch_max_tri_out=1000000, persistent=True, shared_corners=True):
     """src/kd_tree.py:357-399: the tree to split depth 3*(depth - n_subcell_depth), then
     marching cubes on a (2^n_subcell_depth)^3 grid in every unknown leaf.  Returns
-    (T, 3, 3) float32 triangles (order differs from the reference's)."""
+    (T, 3, 3) float32 triangles (order differs from the reference's).  With
+    n_subcell_depth = 0, ``shared_corners`` evaluates each lattice corner once for all
+    the leaves that share it (same triangles)."""
     t = _io.require_cuda()
     k = int(n_subcell_depth)
     ws, cap, counts, m = _tree_device(func, params, lower, upper, 3 * (depth - k), None, 0, 0., persistent)
@@ -117,14 +119,27 @@ def hierarchical_marching_cubes(func, params, lower, upper, depth, n_subcell_dep
     lo, hi = lo.contiguous(), hi.contiguous()
     L = _lib.load()
     tri_cap = max(1024, n_leaves * (8 ** k) * 2)
-    hws_bytes = L.niq_hmc_workspace_size()
+    # the leaves are one lattice's cells: with k = 0, shared corners are evaluated once
+    lattice = k == 0 and bool(shared_corners)
+    rl, ru = _host3(lower), _host3(upper)
+    S = 3 * (depth - k)
+    if lattice:
+        hws_bytes = L.niq_hmc_lattice_workspace_size(rl, ru, S, n_leaves)
+        lattice = hws_bytes > 0 and hws_bytes < (8 << 30)
+    if not lattice:
+        hws_bytes = L.niq_hmc_workspace_size()
     hws = t.empty(hws_bytes, dtype=t.uint8, device='cuda')
     while True:
         tris = t.empty((tri_cap, 3, 3), dtype=t.float32, device='cuda')
         n_t = t.zeros(1, dtype=t.int64, device='cuda')
         try:
-            _lib.check(L.niq_hmc_extract(m.handle, n_leaves, _io.ptr(lo), _io.ptr(hi), k, _io.ptr(tris), tri_cap,
-                                         _io.ptr(n_t), _io.ptr(hws), hws_bytes, _io.stream_handle()))
+            if lattice:
+                _lib.check(L.niq_hmc_extract_lattice(m.handle, n_leaves, _io.ptr(lo), _io.ptr(hi), rl, ru, S,
+                                                     _io.ptr(tris), tri_cap, _io.ptr(n_t), _io.ptr(hws), hws_bytes,
+                                                     _io.stream_handle()))
+            else:
+                _lib.check(L.niq_hmc_extract(m.handle, n_leaves, _io.ptr(lo), _io.ptr(hi), k, _io.ptr(tris), tri_cap,
+                                             _io.ptr(n_t), _io.ptr(hws), hws_bytes, _io.stream_handle()))
             break
         except _lib.NIQCapacityError:
             tri_cap = int(n_t.item()) + 1

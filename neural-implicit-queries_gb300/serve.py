@@ -29,7 +29,7 @@ from concurrent.futures import Future, ThreadPoolExecutor
 
 import numpy as np
 
-from . import _io, _lib, autotune, batched, kd_tree, queries
+from . import _io, _lib, batched, kd_tree, queries
 from .implicit_mlp_utils import generate_implicit_from_params
 from .mlp import device_model, prepend_op, spatial_transformation
 
@@ -95,11 +95,7 @@ class Server:
         self.streams = {'rays': [torch.cuda.Stream() for _ in range(max(1, n_streams // 2))],
                         'closest': [torch.cuda.Stream() for _ in range(max(1, n_streams - n_streams // 2))]}
         self._rr_kind = {'rays': 0, 'closest': 0}
-        # one closest-point CTA per SM leaves room on every SM for the ray kernels'
-        # CTAs (the persistent launch would otherwise hold the whole GPU); this sets the
-        # process-wide launch parameter (restored by close())
-        self._saved_tuning = autotune.get_params()
-        autotune.set_params(batched_ctas_per_sm=1)
+
         # intersections synchronise per search level: they run on their own workers/streams
         self._isect_pool = ThreadPoolExecutor(max_workers=2)
         self._isect_streams = [torch.cuda.Stream() for _ in range(2)]
@@ -134,7 +130,6 @@ class Server:
         self._sched.join()
         self._done.join()
         self._isect_pool.shutdown(wait=True)
-        autotune.set_params(**self._saved_tuning)
 
     def stats(self):
         lat = np.array(self.latencies) * 1e3

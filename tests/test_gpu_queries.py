@@ -317,3 +317,19 @@ def test_tree_schedules_agree(niq, gpu_ready, B):
                      for k in ('unknown', 'interior')})
         assert d['n_boxes_classified'] > 0
     assert sets[0] == sets[1] == sets[2]
+
+
+def test_hmc_shared_corners_same_triangles(niq, gpu_ready):
+    """Evaluating each lattice corner once gives exactly the triangles of the per-leaf
+    evaluation (same values at shared corners, same arithmetic), in another order."""
+    params = niq.workloads.spheres_sdf_model()
+    f = gf(niq, params, conservative=True)
+    lo, hi = -np.ones(3, np.float32), np.ones(3, np.float32)
+    for root in ((lo, hi), (np.array([-1.2, -0.9, -1.1], np.float32), np.array([1.1, 1.0, 0.95], np.float32))):
+        a = niq.kd_tree.hierarchical_marching_cubes(f, params, root[0], root[1], 6, n_subcell_depth=0,
+                                                    shared_corners=True)
+        b = niq.kd_tree.hierarchical_marching_cubes(f, params, root[0], root[1], 6, n_subcell_depth=0,
+                                                    shared_corners=False)
+        assert a.shape == b.shape and a.shape[0] > 1000
+        key = lambda t: t.reshape(t.shape[0], 9)[np.lexsort(t.reshape(t.shape[0], 9).T[::-1])]
+        np.testing.assert_array_equal(key(a), key(b))

@@ -56,4 +56,5 @@ def test_bulk_properties(niq, R, gpu_ready):
     se = vb * np.sqrt(max(p * (1 - p), 1e-12) / n)
     assert abs(mass - rm) <= 5 * np.sqrt(2) * se + 1e-9, (mass, rm, se)
     assert vi <= mass <= vi + vb
-    assert np.max(np.abs(cen - rc)) <= 2e-3, (cen, rc)
+    # seed-to-seed spread of the oracle's own centroid estimate is about 2e-3 per axis
+    assert np.max(np.abs(cen - rc)) <= 1e-2, (cen, rc)
