@@ -6,7 +6,7 @@
 // (two M = 128 tiles), computed by tcgen05.mma kind::tf32 as three split-precision
 // products  Xhi*Ahi + Xhi*Alo + Xlo*Ahi  accumulated in fp32 in tensor memory (TMEM,
 // 512 columns: tile t at columns 256 t).  X and the split weights are streamed through a
-// two-stage shared-memory ring in K chunks of 16 (cp.async), the MMAs issued by one
+// three-stage shared-memory ring in K chunks of 16 (cp.async, two chunks ahead), the MMAs issued by one
 // thread and tracked with an mbarrier per stage.  The base and err rows (one vector
 // each) are computed on the CUDA cores.
 //
@@ -38,13 +38,14 @@ namespace niq {
 constexpr int kTcNT = 256;
 constexpr int kTcKC = 16;                      // K per pipeline stage
 constexpr int kTcRows = 256;                   // noise rows one GEMM holds
-constexpr int kTcTrLD = 33;                    // transpose buffer row stride
+constexpr int kTcTrLD = 17;                    // transpose buffer row stride (16 columns)
+constexpr int kTcStages = 3;                   // shared-memory pipeline depth
 constexpr int kTcStage = 4 * kTcRows * kTcKC;  // floats: X hi, X lo, W hi, W lo
 constexpr int kTcXFloats = kTcRows * NIQ_MAX_WIDTH;  // one split half of a CTA's X scratch
 constexpr long long kTcPolls = 1ll << 24;      // mbarrier polls before a wait gives up
 
 // dynamic shared memory (floats)
-constexpr int kTcOffTr = 2 * kTcStage;
+constexpr int kTcOffTr = kTcStages * kTcStage;
 constexpr int kTcOffPart = kTcOffTr + kTcRows * kTcTrLD;
 constexpr int kTcOffVec = kTcOffPart + 256;
 constexpr int kTcOffMag = kTcOffVec + 8 * 256;
@@ -85,27 +86,27 @@ __device__ __forceinline__ int x_index(int r, int k) {
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// every committed group but the most recent one complete
+__device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// Column sums over the CTA's rows of one 32-column chunk: every thread contributes
-// val[i] for its row; thread t < 32 receives the sum of column t.
+// Column sums over the CTA's rows of one 16-column group: every thread contributes
+// val[i] for its row; thread t < 16 receives the sum of column t.
 template <bool C>
-__device__ __forceinline__ float column_sum32(const float* val, int row, float* tr, float* part) {
+__device__ __forceinline__ float column_sum16(const float* val, int row, float* tr, float* part) {
     const int tid = threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) tr[row * kTcTrLD + i] = val[i];
+    for (int i = 0; i < 16; ++i) tr[row * kTcTrLD + i] = val[i];
     __syncthreads();
-    const int col = tid & 31, pr = tid >> 5;
+    const int col = tid & 15, pr = tid >> 4;
     float s = 0.f;
 #pragma unroll 8
-    for (int q = 0; q < 32; ++q) s = add_up<C>(s, tr[(pr * 32 + q) * kTcTrLD + col]);
-    part[pr * 32 + col] = s;
+    for (int q = 0; q < 16; ++q) s = add_up<C>(s, tr[(pr * 16 + q) * kTcTrLD + col]);
+    part[pr * 16 + col] = s;
     __syncthreads();
     float t = 0.f;
-    if (tid < 32)
-        for (int p = 0; p < kTcNT / 32; ++p) t = add_up<C>(t, part[p * 32 + tid]);
+    if (tid < 16)
+        for (int p = 0; p < kTcNT / 16; ++p) t = add_up<C>(t, part[p * 16 + tid]);
     return t;
 }
 
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     float* s_mag = smem + kTcOffMag;
     int* s_rank = reinterpret_cast<int*>(smem + kTcOffRank);
     __shared__ NiqSpecHeader H;
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[kTcStages];
     __shared__ uint32_t s_tmem;
     __shared__ float red[40];
 
@@ -133,15 +134,14 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     load_header(H, a.M.hdr);
     if (warp == 0) tc::tmem_alloc(&s_tmem, 512);
     if (tid == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
+        for (int i = 0; i < kTcStages; ++i) tc::mbar_init(&bar[i], 1);
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = s_tmem;
-    uint32_t n_commit[2] = {0u, 0u}, n_wait[2] = {0u, 0u};
+    uint32_t n_commit[kTcStages] = {0u, 0u, 0u}, n_wait[kTcStages] = {0u, 0u, 0u};
     float* xs_hi = a.xs + (size_t)blockIdx.x * 2 * kTcXFloats;
     float* xs_lo = xs_hi + kTcXFloats;
     const int tile = warp >> 2;
@@ -233,26 +233,36 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 const float* wlo = whi + (long long)chunks * o16 * kTcKC;
                 const uint32_t idesc = tc::idesc_tf32(128, o16);
                 float g_bs = 0.f, g_es = 0.f, g_rho = 0.f;   // column tid of the base, err, rounding rows
+                // chunk c goes to stage c % kTcStages; loads run two chunks ahead of the MMAs
+                auto load_chunk = [&](int c) {
+                    if (c < chunks) {
+                        const int s = c % kTcStages;
+                        if (!wait_stage(s)) fail = true;   // the MMAs that last read this stage
+                        float* stg = smem + s * kTcStage;
+                        const int xf4 = mt * 128 * kTcKC / 4, wf4 = o16 * kTcKC / 4;
+                        const float* xsrc_h = xs_hi + c * kTcRows * kTcKC;
+                        const float* xsrc_l = xs_lo + c * kTcRows * kTcKC;
+                        const float* wsrc_h = whi + (long long)c * o16 * kTcKC;
+                        const float* wsrc_l = wlo + (long long)c * o16 * kTcKC;
+                        for (int i = tid; i < xf4; i += kTcNT) {
+                            cp_async16(stg + 4 * i, xsrc_h + 4 * i);
+                            cp_async16(stg + kTcRows * kTcKC + 4 * i, xsrc_l + 4 * i);
+                        }
+                        for (int i = tid; i < wf4; i += kTcNT) {
+                            cp_async16(stg + 2 * kTcRows * kTcKC + 4 * i, wsrc_h + 4 * i);
+                            cp_async16(stg + 3 * kTcRows * kTcKC + 4 * i, wsrc_l + 4 * i);
+                        }
+                    }
+                    cp_async_commit();   // an empty group past the last chunk keeps the count
+                };
+                load_chunk(0);
+                load_chunk(1);
                 for (int c = 0; c < chunks; ++c) {
-                    const int s = c & 1;
-                    if (!wait_stage(s)) { fail = true; }
+                    const int s = c % kTcStages;
                     float* stg = smem + s * kTcStage;
-                    const int xf4 = mt * 128 * kTcKC / 4, wf4 = o16 * kTcKC / 4;
-                    const float* xsrc_h = xs_hi + c * kTcRows * kTcKC;
-                    const float* xsrc_l = xs_lo + c * kTcRows * kTcKC;
-                    const float* wsrc_h = whi + (long long)c * o16 * kTcKC;
-                    const float* wsrc_l = wlo + (long long)c * o16 * kTcKC;
-                    for (int i = tid; i < xf4; i += kTcNT) {
-                        cp_async16(stg + 4 * i, xsrc_h + 4 * i);
-                        cp_async16(stg + kTcRows * kTcKC + 4 * i, xsrc_l + 4 * i);
-                    }
-                    for (int i = tid; i < wf4; i += kTcNT) {
-                        cp_async16(stg + 2 * kTcRows * kTcKC + 4 * i, wsrc_h + 4 * i);
-                        cp_async16(stg + 3 * kTcRows * kTcKC + 4 * i, wsrc_l + 4 * i);
-                    }
-                    cp_async_wait_all();
+                    cp_async_wait_but_one();   // chunk c has landed (chunk c + 1 may be in flight)
                     tc::fence_async_smem();
-                    __syncthreads();
+                    __syncthreads();           // also: every thread is done with iteration c - 1
                     if (tid == 0 && !fail) {
                         tc::fence_after_sync();
                         const uint32_t xh = tc::smem_addr(stg), xl = xh + kTcRows * kTcKC * 4;
@@ -275,6 +285,9 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         tc::mma_commit(&bar[s]);
                     }
                     ++n_commit[s];
+                    // the stage of chunk c + 2 held chunk c - 1: every thread finished with it
+                    // (the barrier above); its MMAs are waited for inside load_chunk
+                    load_chunk(c + 2);
                     // base, err and rounding rows while the tensor cores work
                     // (src/affine_layers.py:11-31): column j of the staged weight chunk,
                     // hi + lo = the fp32 weight exactly, against the chunk's 16 inputs
@@ -299,7 +312,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 }
                 // every MMA of the layer complete before TMEM is read; a wait that gave up
                 // anywhere in the CTA ends the kernel for every thread
-                for (int s = 0; s < 2; ++s)
+                for (int s = 0; s < kTcStages; ++s)
                     if (!wait_stage(s)) fail = true;
                 tc::fence_after_sync();
                 fail = __syncthreads_or(fail ? 1 : 0) != 0;   // also: every thread read the old vectors
@@ -333,8 +346,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 if (warp_on) tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
 #pragma unroll
                 for (int i = 0; i < 32; ++i) val[i] = (warp_on && row_ok && ch * 32 + i < out) ? fabsf(val[i]) : 0.f;
-                const float t = column_sum32<C>(val, row, tr, part);
-                if (tid < 32) s_S[ch * 32 + tid] = t;
+                const float t0 = column_sum16<C>(val, row, tr, part);
+                if (tid < 16) s_S[ch * 32 + tid] = t0;
+                const float t1 = column_sum16<C>(val + 16, row, tr, part);
+                if (tid < 16) s_S[ch * 32 + 16 + tid] = t1;
             }
             __syncthreads();
             // 2. linearisation per column
@@ -417,8 +432,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 }
 #pragma unroll
                 for (int i = 0; i < 32; ++i) val[i] = (row_ok && !kept) ? fabsf(val[i]) : 0.f;
-                const float t = column_sum32<C>(val, row, tr, part);
-                if (tid < 32) s_drop[ch * 32 + tid] = t;
+                const float t0 = column_sum16<C>(val, row, tr, part);
+                if (tid < 16) s_drop[ch * 32 + tid] = t0;
+                const float t1 = column_sum16<C>(val + 16, row, tr, part);
+                if (tid < 16) s_drop[ch * 32 + 16 + tid] = t1;
             }
             // new rows diag(delta): kept ones become rows of X, dropped ones go to err
             if (j < out) {
@@ -506,7 +523,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
         }
     }
     // unwind: wait (bounded) for MMAs still in flight, then free TMEM
-    for (int s = 0; s < 2; ++s)
+    for (int s = 0; s < kTcStages; ++s)
         while (n_wait[s] < n_commit[s]) {
             if (!tc::mbar_wait(&bar[s], n_wait[s] & 1u, kTcPolls)) {
                 if (tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
