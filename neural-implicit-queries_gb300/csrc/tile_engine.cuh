@@ -288,11 +288,14 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
     for (int li = 0; li < nl; ++li) {
         const NiqLayer L = H.layers[li];
         const bool last = (li + 1 == nl);
-        float acc[R][COLS];
+        // accumulators in column pairs: the dense loop updates both columns of a pair with
+        // one packed FMA (two correctly rounded fp32 FMAs in one instruction)
+        float2 acc2[R][COLS / 2];
+#define ACC(r, c) (((c) & 1) ? acc2[r][(c) >> 1].y : acc2[r][(c) >> 1].x)
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < COLS; ++c) acc[r][c] = 0.f;
+            for (int c = 0; c < COLS / 2; ++c) acc2[r][c] = make_float2(0.f, 0.f);
 
         bool qv[NQ];
 #pragma unroll
@@ -328,7 +331,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                         const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
 #pragma unroll
                         for (int c = 0; c < 4; ++c)
-                            acc[r][c] = fmaf(xv, r < R - NABS ? a[c] : fabsf(a[c]), acc[r][c]);
+                            ACC(r, c) = fmaf(xv, r < R - NABS ? a[c] : fabsf(a[c]), ACC(r, c));
                     }
                 }
             }
@@ -338,13 +341,13 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
 #pragma unroll
                 for (int r = 0; r < R; ++r)
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[r][c] += __shfl_xor_sync(0xffffffffu, acc[r][c], off);
+                    for (int c = 0; c < 4; ++c) ACC(r, c) += __shfl_xor_sync(0xffffffffu, ACC(r, c), off);
             // lanes g > 0 now hold copies; only g == 0 owns column group 0 below
             if (g != 0) {
 #pragma unroll
                 for (int r = 0; r < R; ++r)
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
+                    for (int c = 0; c < 4; ++c) ACC(r, c) = 0.f;
             }
         }
 
@@ -380,16 +383,19 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                                           : make_float4(0.f, 0.f, 0.f, 0.f);
                         a[4 * q + 0] = av.x; a[4 * q + 1] = av.y; a[4 * q + 2] = av.z; a[4 * q + 3] = av.w;
                     }
+                    float2 w[COLS / 2], wa[COLS / 2];
+#pragma unroll
+                    for (int c = 0; c < COLS / 2; ++c) {
+                        w[c] = make_float2(a[2 * c], a[2 * c + 1]);
+                        if (NABS > 0) wa[c] = make_float2(fabsf(a[2 * c]), fabsf(a[2 * c + 1]));
+                    }
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
                         const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
-                        if (r < R - NABS) {
+                        const float2 x2 = make_float2(xv, xv);
 #pragma unroll
-                            for (int c = 0; c < COLS; ++c) acc[r][c] = fmaf(xv, a[c], acc[r][c]);
-                        } else {
-#pragma unroll
-                            for (int c = 0; c < COLS; ++c) acc[r][c] = fmaf(xv, fabsf(a[c]), acc[r][c]);
-                        }
+                        for (int c = 0; c < COLS / 2; ++c)
+                            acc2[r][c] = __ffma2_rn(x2, r < R - NABS ? w[c] : wa[c], acc2[r][c]);
                     }
                 }
             }
@@ -417,7 +423,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                 const float b = live ? bsrc[col] : 0.f;
                 float v[R];
 #pragma unroll
-                for (int r = 0; r < R; ++r) v[r] = acc[r][c];
+                for (int r = 0; r < R; ++r) v[r] = ACC(r, c);
 
                 if (plan.mode == ROWS_POINTS) {
 #pragma unroll
@@ -527,7 +533,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                     }
                 } else {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) acc[r][c] = v[r];
+                    for (int r = 0; r < R; ++r) ACC(r, c) = v[r];
                 }
             }
             // one 16-byte store per row for the thread's 4 columns (scalar stores of
@@ -537,13 +543,14 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     *reinterpret_cast<float4*>(xs + r * LD + col0) =
-                        make_float4(acc[r][4 * q], acc[r][4 * q + 1], acc[r][4 * q + 2], acc[r][4 * q + 3]);
+                        make_float4(acc2[r][2 * q].x, acc2[r][2 * q].y, acc2[r][2 * q + 1].x, acc2[r][2 * q + 1].y);
             }
         }
         // layer output visible before the next layer reads it (the item's own warp), and
         // after the last layer, every item's `out` row visible to the whole block
         if (last && !WARP) __syncthreads();
         else __syncwarp();
+#undef ACC
     }
 }
 
