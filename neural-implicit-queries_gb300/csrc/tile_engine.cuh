@@ -260,6 +260,20 @@ __device__ __forceinline__ void stage_floats(float* __restrict__ dst, const floa
 // Floats needed to hold one layer's weights (A then b).
 NIQ_HOST_DEVICE int layer_floats(const NiqLayer& L) { return L.in_pad * L.out_pad + L.out_pad; }
 
+// Per-thread accumulator tile: R rows x COLS columns, stored in column pairs when the
+// dense loop uses packed FMAs (PK) and as plain floats otherwise.
+template <int R, int COLS, bool PK>
+struct AccTile {
+    float v[R][COLS];
+    __device__ __forceinline__ float& at(int r, int c) { return v[r][c]; }
+};
+template <int R, int COLS>
+struct AccTile<R, COLS, true> {
+    float2 v[R][COLS / 2];
+    __device__ __forceinline__ float& at(int r, int c) { return (c & 1) ? v[r][c >> 1].y : v[r][c >> 1].x; }
+    __device__ __forceinline__ float2& pair(int r, int c2) { return v[r][c2]; }
+};
+
 // ----------------------------------------------------------------------------------
 // The fused forward pass.
 //
@@ -288,14 +302,14 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
     for (int li = 0; li < nl; ++li) {
         const NiqLayer L = H.layers[li];
         const bool last = (li + 1 == nl);
-        // accumulators in column pairs: the dense loop updates both columns of a pair with
+        // accumulators; for bound rows in column pairs, which the dense loop updates with
         // one packed FMA (two correctly rounded fp32 FMAs in one instruction)
-        float2 acc2[R][COLS / 2];
-#define ACC(r, c) (((c) & 1) ? acc2[r][(c) >> 1].y : acc2[r][(c) >> 1].x)
+        AccTile<R, COLS, (NABS > 0)> acc;
+#define ACC(r, c) acc.at(r, c)
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < COLS / 2; ++c) acc2[r][c] = make_float2(0.f, 0.f);
+            for (int c = 0; c < COLS; ++c) ACC(r, c) = 0.f;
 
         bool qv[NQ];
 #pragma unroll
@@ -383,19 +397,31 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                                           : make_float4(0.f, 0.f, 0.f, 0.f);
                         a[4 * q + 0] = av.x; a[4 * q + 1] = av.y; a[4 * q + 2] = av.z; a[4 * q + 3] = av.w;
                     }
-                    float2 w[COLS / 2], wa[COLS / 2];
+                    if constexpr (NABS > 0) {
+                        // bound rows: issue-bound, so packed FMAs pay for the pair rebuilt
+                        // from each input value
+                        float2 w[COLS / 2], wa[COLS / 2];
 #pragma unroll
-                    for (int c = 0; c < COLS / 2; ++c) {
-                        w[c] = make_float2(a[2 * c], a[2 * c + 1]);
-                        if (NABS > 0) wa[c] = make_float2(fabsf(a[2 * c]), fabsf(a[2 * c + 1]));
-                    }
+                        for (int c = 0; c < COLS / 2; ++c) {
+                            w[c] = make_float2(a[2 * c], a[2 * c + 1]);
+                            wa[c] = make_float2(fabsf(a[2 * c]), fabsf(a[2 * c + 1]));
+                        }
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
-                        const float2 x2 = make_float2(xv, xv);
+                        for (int r = 0; r < R; ++r) {
+                            const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
+                            const float2 x2 = make_float2(xv, xv);
 #pragma unroll
-                        for (int c = 0; c < COLS / 2; ++c)
-                            acc2[r][c] = __ffma2_rn(x2, r < R - NABS ? w[c] : wa[c], acc2[r][c]);
+                            for (int c = 0; c < COLS / 2; ++c)
+                                acc.pair(r, c) = __ffma2_rn(x2, r < R - NABS ? w[c] : wa[c], acc.pair(r, c));
+                        }
+                    } else {
+                        // point rows only: plain FMAs (no pair to rebuild per input value)
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c) ACC(r, c) = fmaf(xv, a[c], ACC(r, c));
+                        }
                     }
                 }
             }
@@ -543,7 +569,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     *reinterpret_cast<float4*>(xs + r * LD + col0) =
-                        make_float4(acc2[r][2 * q].x, acc2[r][2 * q].y, acc2[r][2 * q + 1].x, acc2[r][2 * q + 1].y);
+                        make_float4(ACC(r, 4 * q), ACC(r, 4 * q + 1), ACC(r, 4 * q + 2), ACC(r, 4 * q + 3));
             }
         }
         // layer output visible before the next layer reads it (the item's own warp), and
