@@ -125,7 +125,7 @@ static int launch_tile_kernel(K kernel, int R, int TPI, const niq_model* m, long
     const int items = kNT / TPI;
     const int W = TPI * 8;
     const int state = items * R * (W + 4) + ((items * R + 3) & ~3);
-    p = plan_smem(state, m->hdr.n_weight_floats, max_layer_floats(m->hdr));
+    p = plan_smem(state, m->hdr.n_weight_floats, max_layer_floats(m->hdr), smem_budget(kernel, kNT));
     int rc = prepare_kernel(kernel, p.bytes);
     if (rc) return rc;
     return persistent_grid(kernel, kNT, p.bytes, work_tiles, &grid);

@@ -440,7 +440,7 @@ int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bo
     auto run = [&](auto kern, int TPIv) -> int {
         const int items = kNT / TPIv;
         const int state = items * 8 * (TPIv * 8 + 4) + ((items * 8 + 3) & ~3);
-        SmemPlan p = plan_smem(state, wfloats, maxlayer);
+        SmemPlan p = plan_smem(state, wfloats, maxlayer, smem_budget(kern, kNT));
         NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * maxw, NIQ_ERR_UNSUPPORTED, "shared memory too small for width %d", maxw);
         int r2 = prepare_kernel(kern, p.bytes);
         if (r2) return r2;

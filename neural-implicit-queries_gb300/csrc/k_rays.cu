@@ -462,7 +462,7 @@ int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts*
     auto run = [&](auto kern, int R, int TPIv) -> int {
         const int items = kNT / TPIv;
         const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
-        SmemPlan p = plan_smem(state, wfloats, maxlayer);
+        SmemPlan p = plan_smem(state, wfloats, maxlayer, smem_budget(kern, kNT));
         NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * maxw, NIQ_ERR_UNSUPPORTED, "shared memory too small for width %d", maxw);
         int r2 = prepare_kernel(kern, p.bytes);
         if (r2) return r2;

@@ -687,7 +687,7 @@ template <class K>
 int cp_plan(K kern, const niq_model* m, int R, int TPIv, SmemPlan& p) {
     const int items = kNT / TPIv;
     const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
-    p = plan_smem(state, m->hdr.n_weight_floats, max_layer_floats(m->hdr));
+    p = plan_smem(state, m->hdr.n_weight_floats, max_layer_floats(m->hdr), smem_budget(kern, kNT));
     NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * m->hdr.max_width, NIQ_ERR_UNSUPPORTED, "shared memory too small");
     return prepare_kernel(kern, p.bytes);
 }
@@ -890,7 +890,7 @@ int niq_find_any_intersection(const niq_model* model_a, const niq_model* model_b
         auto run = [&](auto kern, int TPIv) -> int {
             const int items = kNT / TPIv;
             const int state = items * 8 * (TPIv * 8 + 4) + ((items * 8 + 3) & ~3);
-            SmemPlan p = plan_smem(state, wfl, ml);
+            SmemPlan p = plan_smem(state, wfl, ml, smem_budget(kern, kNT));
             NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * maxw, NIQ_ERR_UNSUPPORTED, "shared memory too small");
             int r2 = prepare_kernel(kern, p.bytes);
             if (r2) return r2;

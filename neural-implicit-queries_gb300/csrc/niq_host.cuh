@@ -80,6 +80,20 @@ inline SmemPlan plan_smem(int fixed_floats, int weight_floats, int max_layer, in
     return p;
 }
 
+// Shared-memory budget of one CTA of `nt` threads: kSmemBudget while the kernel's
+// registers let two CTAs share an SM, else (one CTA per SM anyway) the per-block maximum,
+// so that the weights can stay resident instead of being restaged every layer.
+template <class K>
+inline int smem_budget(K kernel, int nt) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return kSmemBudget;
+    const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;   // allocated per warp in units of 256
+    if (2 * warp_regs * (nt / 32) <= 65536) return kSmemBudget;
+    const DeviceInfo& d = device_info();
+    const int b = d.smem_optin - (int)fa.sharedSizeBytes;
+    return b > kSmemBudget ? b : kSmemBudget;
+}
+
 template <class K>
 inline int prepare_kernel(K kernel, size_t smem) {
     NIQ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
