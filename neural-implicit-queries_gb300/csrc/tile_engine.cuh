@@ -88,22 +88,23 @@ __device__ __forceinline__ Lin lin_relu(float l, float u) {
     }
     // Conservative: any alpha in [0, 1] gives a valid enclosure, because the offset
     // interval below is computed for the alpha actually used.  So the secant slope
-    // u / (u - l) (l < 0 <= u) takes the fast divide (within 2 ulp, no slow path), and
-    // the cases are selects rather than branches.
-    const bool straddle = (l < 0.f) && (u >= 0.f);
-    float a = (l >= 0.f) ? 1.f : (straddle ? __fdividef(u, __fsub_rn(u, l)) : 0.f);
-    a = fminf(fmaxf(a, 0.f), 1.f);  // NaN -> 0 (fmaxf drops NaN), clip to [0, 1]
-    r.a = a;
-    // g(x) = relu(x) - a x is piecewise linear: extrema at l, u and 0 (l < 0 <= u); it is
-    // exactly 0 (identity, a = 1) or relu(x) = 0 (a = 0) otherwise
-    const float gl_lo = __fmul_rd(-a, l), gl_hi = __fmul_ru(-a, l);
-    const float gu_lo = __fmaf_rd(-a, u, u), gu_hi = __fmaf_ru(-a, u, u);
-    const float rlo = fminf(fminf(gl_lo, gu_lo), 0.f);
-    const float rhi = fmaxf(fmaxf(gl_hi, gu_hi), 0.f);
-    const float b = 0.5f * (rlo + rhi);
-    r.b = straddle ? b : 0.f;
-    // a NaN bound (overflowed input) leaves nothing known: unbounded offset
-    r.d = straddle ? fmaxf(__fsub_ru(rhi, b), __fsub_ru(b, rlo)) : ((l == l && u == u) ? 0.f : INFINITY);
+    // u / (u - l) (l < 0 <= u) takes the fast divide (within 2 ulp, no slow path).
+    // Otherwise g(x) = relu(x) - a x is exactly 0 (identity, a = 1) or relu(x) = 0
+    // (a = 0); a NaN bound (overflowed input) leaves nothing known: unbounded offset.
+    r.a = (l >= 0.f) ? 1.f : 0.f;
+    r.b = 0.f;
+    r.d = (l == l && u == u) ? 0.f : INFINITY;
+    if ((l < 0.f) && (u >= 0.f)) {
+        const float a = fminf(fmaxf(__fdividef(u, __fsub_rn(u, l)), 0.f), 1.f);  // NaN -> 0
+        r.a = a;
+        // g is piecewise linear here: extrema at l, u and 0
+        const float gl_lo = __fmul_rd(-a, l), gl_hi = __fmul_ru(-a, l);
+        const float gu_lo = __fmaf_rd(-a, u, u), gu_hi = __fmaf_ru(-a, u, u);
+        const float rlo = fminf(fminf(gl_lo, gu_lo), 0.f);
+        const float rhi = fmaxf(fmaxf(gl_hi, gu_hi), 0.f);
+        r.b = 0.5f * (rlo + rhi);
+        r.d = fmaxf(__fsub_ru(rhi, r.b), __fsub_ru(r.b, rlo));
+    }
     return r;
 }
 
