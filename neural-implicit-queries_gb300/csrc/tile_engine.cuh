@@ -449,6 +449,73 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
         const float tiny = (float)(L.in + 2) * NIQ_TINY;
         const int act = L.act;
 
+        // Affine rows of an activated hidden layer: the same rules as the general loop
+        // below, done in three passes over each group of 4 columns (bounds, then the
+        // linearisations, then the updates), so that the branch-free passes of
+        // different columns overlap instead of each column's chain running alone.
+        constexpr bool AFFINE_TILE = (R == 5 && NABS == 1);
+        const bool phased = AFFINE_TILE && plan.mode == ROWS_AFFINE && plan.np == 0 && !last && act != NIQ_ACT_NONE;
+        if (phased) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            if (!qv[q]) continue;
+            float base4[4], err4[4], S4[4], lo4[4], hi4[4];
+            bool live4[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = 4 * q + j;
+                const int col = col_of<TPI>(g, q) + j;
+                live4[j] = col < L.out;
+                const float b = live4[j] ? bsrc[col] : 0.f;
+                base4[j] = __fadd_rn(ACC(0, c), b);
+                float err = ACC(R - 1, c);
+                if (C) err = __fadd_ru(__fmaf_ru(err, scale, __fmul_ru(gam, fabsf(b))), tiny);
+                err4[j] = err;
+                float S = 0.f;
+#pragma unroll
+                for (int r = 1; r < R - 1; ++r)
+                    if (r <= plan.v) S = add_up<C>(S, fabsf(ACC(r, c)));
+                S4[j] = S;
+                const float rad = add_up<C>(S, err);
+                lo4[j] = sub_dn<C>(base4[j], rad);
+                hi4[j] = add_up<C>(base4[j], rad);
+            }
+            Lin z4[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) z4[j] = linearize<C>(act, lo4[j], hi4[j]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = 4 * q + j;
+                const Lin z = z4[j];
+                float base = base4[j], err = err4[j];
+                const float nb = C ? fmaf(z.a, base, z.b) : __fadd_rn(__fmul_rn(z.a, base), z.b);
+#pragma unroll
+                for (int r = 1; r < R - 1; ++r)
+                    if (r <= plan.v) ACC(r, c) = __fmul_rn(z.a, ACC(r, c));
+                if (C) {
+                    const float aS = __fmul_ru(z.a, S4[j]);
+                    err = __fmaf_ru(z.a, err, z.d);
+                    err = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, err);
+                    base = nb;
+                    err = __fmaf_ru(gam_next, __fadd_ru(fabsf(base), __fmul_ru(aS, 1.f + NIQ_ULP_REL)), err);
+                } else {
+                    err = __fadd_rn(__fmul_rn(z.a, err), z.d);
+                    base = nb;
+                }
+                ACC(0, c) = base;
+                ACC(R - 1, c) = err;
+                if (!live4[j]) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) ACC(r, c) = 0.f;
+                }
+            }
+            const int col0 = col_of<TPI>(g, q);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                *reinterpret_cast<float4*>(xs + r * LD + col0) =
+                    make_float4(ACC(r, 4 * q), ACC(r, 4 * q + 1), ACC(r, 4 * q + 2), ACC(r, 4 * q + 3));
+        }
+        } else {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
 #pragma unroll
@@ -583,6 +650,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                         make_float4(ACC(r, 4 * q), ACC(r, 4 * q + 1), ACC(r, 4 * q + 2), ACC(r, 4 * q + 3));
             }
         }
+        }  // general epilogue
         // layer output visible before the next layer reads it (the item's own warp), and
         // after the last layer, every item's `out` row visible to the whole block
         if (last && !WARP) __syncthreads();
