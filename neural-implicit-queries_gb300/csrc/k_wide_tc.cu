@@ -141,7 +141,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = s_tmem;
-    uint32_t n_commit[kTcStages] = {0u, 0u, 0u}, n_wait[kTcStages] = {0u, 0u, 0u};
+    // A stage has at most one MMA commit outstanding (it is waited for before reuse):
+    // bit s of `pending` marks it, bit s of `phase` is the parity of its next completion.
+    // Register bit masks, not arrays indexed by the stage, which would live in local memory.
+    uint32_t pending = 0u, phase = 0u;
     float* xs_hi = a.xs + (size_t)blockIdx.x * 2 * kTcXFloats;
     float* xs_lo = xs_hi + kTcXFloats;
     const int tile = warp >> 2;
@@ -153,9 +156,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     bool fail = false;
 
     auto wait_stage = [&](int s) -> bool {
-        if (n_wait[s] >= n_commit[s]) return true;
-        const bool ok = tc::mbar_wait(&bar[s], n_wait[s] & 1u, kTcPolls);
-        ++n_wait[s];
+        if (!((pending >> s) & 1u)) return true;
+        const bool ok = tc::mbar_wait(&bar[s], (phase >> s) & 1u, kTcPolls);
+        phase ^= 1u << s;
+        pending &= ~(1u << s);
         return ok;
     };
 
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         }
                         tc::mma_commit(&bar[s]);
                     }
-                    ++n_commit[s];
+                    pending |= 1u << s;
                     // the stage of chunk c + 2 held chunk c - 1: every thread finished with it
                     // (the barrier above); its MMAs are waited for inside load_chunk
                     load_chunk(c + 2);
@@ -524,12 +528,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     }
     // unwind: wait (bounded) for MMAs still in flight, then free TMEM
     for (int s = 0; s < kTcStages; ++s)
-        while (n_wait[s] < n_commit[s]) {
-            if (!tc::mbar_wait(&bar[s], n_wait[s] & 1u, kTcPolls)) {
-                if (tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
-            }
-            ++n_wait[s];
-        }
+        if (!wait_stage(s) && tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
