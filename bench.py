@@ -574,7 +574,7 @@ def run_batched(args):
     torch.cuda.synchronize()
     t_p = (time.perf_counter() - t0) * n_models / n_plain
     nq = int(counts.sum())
-    print(json.dumps({"metric": "closest-point queries/s (512 MLPs in one launch)", "value": nq / t_b,
+    print(json.dumps({"metric": f"closest-point queries/s ({n_models} MLPs in one launch)", "value": nq / t_b,
                       "unit": "queries/s", "ms": t_b * 1e3, "queries": nq, "models": n_models,
                       "plain_per_model_calls": {"queries_per_s": nq / t_p, "ms_extrapolated": t_p * 1e3,
                                                 "models_timed": n_plain},

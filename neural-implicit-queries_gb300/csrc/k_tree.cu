@@ -148,17 +148,21 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
                         if (pu < B.cap) put_node(B.res_lo[0], B.res_hi[0], pu, lo, hi);
                         else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
                     } else if (pc + 1 < B.cap) {
-                        // split along the first longest axis (jnp.argmax: first maximum)
-                        const float e0 = __fsub_rn(hi[0], lo[0]), e1 = __fsub_rn(hi[1], lo[1]), e2 = __fsub_rn(hi[2], lo[2]);
+                        // split along the first longest axis (jnp.argmax: first maximum);
+                        // selects rather than a runtime index keep the boxes in registers
+                        const float l0 = lo[0], l1 = lo[1], l2 = lo[2], h0 = hi[0], h1 = hi[1], h2 = hi[2];
+                        const float e0 = __fsub_rn(h0, l0), e1 = __fsub_rn(h1, l1), e2 = __fsub_rn(h2, l2);
                         int d = 0;
                         float em = e0;
                         if (e1 > em) { d = 1; em = e1; }
                         if (e2 > em) { d = 2; }
-                        float alo[3] = {lo[0], lo[1], lo[2]}, ahi[3] = {hi[0], hi[1], hi[2]};
-                        float blo[3] = {lo[0], lo[1], lo[2]}, bhi[3] = {hi[0], hi[1], hi[2]};
-                        const float mid = __fmul_rn(0.5f, __fadd_rn(lo[d], hi[d]));
-                        ahi[d] = mid;
-                        blo[d] = mid;
+                        const float mid = d == 0 ? __fmul_rn(0.5f, __fadd_rn(l0, h0))
+                                        : d == 1 ? __fmul_rn(0.5f, __fadd_rn(l1, h1))
+                                                 : __fmul_rn(0.5f, __fadd_rn(l2, h2));
+                        const float alo[3] = {l0, l1, l2};
+                        const float ahi[3] = {d == 0 ? mid : h0, d == 1 ? mid : h1, d == 2 ? mid : h2};
+                        const float blo[3] = {d == 0 ? mid : l0, d == 1 ? mid : l1, d == 2 ? mid : l2};
+                        const float bhi[3] = {h0, h1, h2};
                         put_node(out_lo, out_hi, pc, alo, ahi);
                         put_node(out_lo, out_hi, pc + 1, blo, bhi);
                     } else {
