@@ -7,7 +7,7 @@ The product path (the CUDA kernels behind ``include/niq.h``) never calls it.
 Every function restates one reference function, vectorised over a leading batch axis
 (where the reference uses ``jax.vmap``) and parameterised by ``dtype``:
 ``np.float32`` mirrors the reference's fp32 JAX arithmetic, ``np.float64`` is the
-FP64 affine-arithmetic oracle used to judge bound widths.
+FP64 affine-arithmetic oracle against which bound widths are measured.
 
 Parity pin: ``tests/golden/make_golden.py`` executes the reference's own ``src/*.py``
 (over a NumPy stand-in for the absent ``jax`` package) on seeded inputs and commits the
