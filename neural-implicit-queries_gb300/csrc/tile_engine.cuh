@@ -449,17 +449,17 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
         const float tiny = (float)(L.in + 2) * NIQ_TINY;
         const int act = L.act;
 
-        // Affine rows of an activated hidden layer: the same rules as the general loop
-        // below, done in three passes over each group of 4 columns (bounds, then the
-        // linearisations, then the updates), so that the branch-free passes of
-        // different columns overlap instead of each column's chain running alone.
-        constexpr bool AFFINE_TILE = (R == 5 && NABS == 1);
-        const bool phased = AFFINE_TILE && plan.mode == ROWS_AFFINE && plan.np == 0 && !last && act != NIQ_ACT_NONE;
+        // Affine rows (and point rows) of an activated hidden layer: the same rules as
+        // the general loop below, done in three passes over each group of 4 columns
+        // (bounds, then the linearisations, then the updates), so that the branch-free
+        // passes of different columns overlap instead of each column's chain running alone.
+        constexpr bool AFFINE_TILE = (NABS == 1);
+        const bool phased = AFFINE_TILE && plan.mode == ROWS_AFFINE && !last && act != NIQ_ACT_NONE;
         if (phased) {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
             if (!qv[q]) continue;
-            float base4[4], err4[4], S4[4], lo4[4], hi4[4];
+            float base4[4], err4[4], S4[4], lo4[4], hi4[4], b4[4];
             bool live4[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -467,6 +467,7 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                 const int col = col_of<TPI>(g, q) + j;
                 live4[j] = col < L.out;
                 const float b = live4[j] ? bsrc[col] : 0.f;
+                b4[j] = b;
                 base4[j] = __fadd_rn(ACC(0, c), b);
                 float err = ACC(R - 1, c);
                 if (C) err = __fadd_ru(__fmaf_ru(err, scale, __fmul_ru(gam, fabsf(b))), tiny);
@@ -490,8 +491,10 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                 float base = base4[j], err = err4[j];
                 const float nb = C ? fmaf(z.a, base, z.b) : __fadd_rn(__fmul_rn(z.a, base), z.b);
 #pragma unroll
-                for (int r = 1; r < R - 1; ++r)
+                for (int r = 1; r < R - 1; ++r) {
                     if (r <= plan.v) ACC(r, c) = __fmul_rn(z.a, ACC(r, c));
+                    else if (r <= plan.v + plan.np) ACC(r, c) = act_point(act, __fadd_rn(ACC(r, c), b4[j]));
+                }
                 if (C) {
                     const float aS = __fmul_ru(z.a, S4[j]);
                     err = __fmaf_ru(z.a, err, z.d);
