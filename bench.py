@@ -278,9 +278,9 @@ def run_ours(args):
                      "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak,
                      # DRAM bytes of one k_tree launch: the ncu capture of the 18-bisection tree
-                     # (profiles/k_tree_k_hmc_spheres64_split18_full.md: 0.444 MB read + 0.191 MB
+                     # (profiles/k_tree_spheres64_split18_full.md: 148.5 KB read + 6.9 KB
                      # written for 332,953 boxes) scaled by boxes to this launch
-                     "traffic": (444160 + 190976) / 332953 * n_boxes,
+                     "traffic": (148480 + 6912) / 332953 * n_boxes,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the "
                                        "18-bisection tree, scaled to this launch's boxes; the level arrays stay in L2",
                      "flops_per_box": bf,
