@@ -90,6 +90,31 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 // every committed group but the most recent one complete
 __device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
+// Stable descending rank of value v at index me among s[0..n):
+//   #{i : s_i > v} + #{i < me : s_i == v}   (the order of a stable descending argsort).
+// Below the calling warp's window [w0, w0 + 32) every index is < me, so the test is
+// s_i >= v; above it every index is > me, so it is s_i > v.  Those two ranges go in
+// float4 steps; only the window compares indices.  s is 16-byte aligned, w0 <= me < n.
+__device__ __forceinline__ int stable_rank(const float* s, int n, float v, int me, int w0) {
+    const int lo = w0 & ~3;
+    int hi = (w0 + 32 + 3) & ~3;
+    if (hi > n) hi = n;
+    int rk = 0;
+    for (int i = 0; i < lo; i += 4) {
+        const float4 q = *reinterpret_cast<const float4*>(s + i);
+        rk += (q.x >= v) + (q.y >= v) + (q.z >= v) + (q.w >= v);
+    }
+    for (int i = lo; i < hi; ++i) rk += (s[i] > v) || (s[i] == v && i < me);
+    const int n4 = n & ~3;
+    int i = hi;
+    for (; i < n4; i += 4) {
+        const float4 q = *reinterpret_cast<const float4*>(s + i);
+        rk += (q.x > v) + (q.y > v) + (q.z > v) + (q.w > v);
+    }
+    for (i = (i > hi ? i : hi); i < n; ++i) rk += s[i] > v;
+    return rk;
+}
+
 // Column sums over the CTA's rows of one 16-column group: every thread contributes
 // val[i] for its row; thread t < 16 receives the sum of column t.
 template <bool C>
@@ -393,17 +418,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 if (j < out) s_mag[nrows + j] = delta;
                 __syncthreads();
                 // 4. stable descending rank
-                if (row_ok) {
-                    int rk = 0;
-                    for (int i = 0; i < ncand; ++i) rk += (s_mag[i] > m) || (s_mag[i] == m && i < row);
-                    s_rank[row] = rk;
-                }
-                if (j < out) {
-                    const int me = nrows + j;
-                    int rk = 0;
-                    for (int i = 0; i < ncand; ++i) rk += (s_mag[i] > delta) || (s_mag[i] == delta && i < me);
-                    s_rank[me] = rk;
-                }
+                if (row_ok) s_rank[row] = stable_rank(s_mag, ncand, m, row, row - lane);
+                if (j < out) s_rank[nrows + j] = stable_rank(s_mag, ncand, delta, nrows + j, nrows + j - lane);
             } else {
                 if (row_ok) s_rank[row] = row;
                 if (j < out) s_rank[nrows + j] = nrows + j;
