@@ -1,6 +1,8 @@
 /* cpu_tree.c -- CPU restatement of the level-set tree (src/kd_tree.py:19-218) over
- * affine_fixed bounds (src/affine.py:109-193, src/affine_layers.py:11-56), in C with
- * OpenMP, for the CPU baseline of the benchmark and as a second checker of the tree.
+ * affine_fixed bounds (src/affine.py:109-193, src/affine_layers.py:11-56) and of the
+ * marching-cubes extraction on its leaves (src/kd_tree.py:357-399 with n_subcell_depth
+ * 0, src/extract_cell.py:314-421), in C with OpenMP, for the CPU baseline of the
+ * benchmark and as a second checker of the tree.
  *
  * Test infrastructure: only the tests and the benchmark's CPU-baseline leg call it.
  *
@@ -188,4 +190,105 @@ int64_t cpu_levelset_tree(int n_layers, const int* in, const int* out, const int
     free(cur);
     if (n_boxes) *n_boxes = boxes;
     return n_leaves;
+}
+
+
+/* Plain forward pass of one point (src/mlp.py:253-347, float32, no contraction). */
+static float eval_point(const Net* N, const float* x) {
+    float a[MAXW], b[MAXW];
+    float* cur = a;
+    float* nxt = b;
+    cur[0] = x[0]; cur[1] = x[1]; cur[2] = x[2];
+    for (int li = 0; li < N->n_layers; ++li) {
+        const int in = N->in[li], out = N->out[li];
+        const float* A = N->A[li];
+        for (int j = 0; j < out; ++j) nxt[j] = 0.f;
+        for (int k = 0; k < in; ++k) {
+            const float xk = cur[k];
+            const float* row = A + (size_t)k * out;
+            for (int j = 0; j < out; ++j) nxt[j] += xk * row[j];
+        }
+        for (int j = 0; j < out; ++j) {
+            float v = nxt[j] + (N->b[li] ? N->b[li][j] : 0.f);
+            if (N->act[li] == 1) v = fmaxf(v, 0.f);
+            else if (N->act[li] == 2) v = eluf_(v);
+            nxt[j] = v;
+        }
+        float* t = cur; cur = nxt; nxt = t;
+    }
+    return cur[0];
+}
+
+/* Marching cubes on each leaf box as one cell (n_subcell_depth 0): the 8 corners
+ * (corner i at vert[i] in {0,1}^3: upper where 1, lower where 0), case bit i set when
+ * the value at corner i is negative, and for every triangle of tri_table[case] (256 x
+ * 16, -1 padded) the vertices on edges (edge[e] = corners a, b) at
+ * t = clip(nan_to_num(-va / (vb - va)), 0, 1), p = (1 - t) pa + t pb.  Returns the number
+ * of triangles; writes up to cap of them to tris (T, 3, 3) in leaf order. */
+int64_t cpu_hmc_leaves(int n_layers, const int* in, const int* out, const int* act, const float* const* A,
+                       const float* const* b, const float* leaves, int64_t n, const int* tri_table, const int* edge,
+                       const int* vert, int threads, float* tris, int64_t cap) {
+    Net N;
+    if (n_layers < 1 || n_layers > MAXL) return -1;
+    N.n_layers = n_layers;
+    for (int i = 0; i < n_layers; ++i) {
+        if (in[i] > MAXW || out[i] > MAXW || act[i] < 0 || act[i] > 2) return -1;
+        N.in[i] = in[i]; N.out[i] = out[i]; N.act[i] = act[i]; N.A[i] = A[i]; N.b[i] = b[i];
+    }
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    float* vals = (float*)malloc((size_t)(n > 0 ? n : 1) * 8 * sizeof(float));
+    int64_t* first = (int64_t*)malloc((size_t)(n + 1) * sizeof(int64_t));
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        const float* lo = leaves + 6 * i;
+        const float* hi = lo + 3;
+        int cs = 0;
+        for (int c = 0; c < 8; ++c) {
+            float p[3];
+            for (int k = 0; k < 3; ++k) p[k] = vert[3 * c + k] ? hi[k] : lo[k];
+            const float v = eval_point(&N, p);
+            vals[8 * i + c] = v;
+            if (v < 0.f) cs |= 1 << c;
+        }
+        int nt = 0;
+        while (nt < 5 && tri_table[16 * cs + 3 * nt] != -1) ++nt;
+        first[i + 1] = nt;
+    }
+    first[0] = 0;
+    for (int64_t i = 0; i < n; ++i) first[i + 1] += first[i];
+    const int64_t total = first[n];
+    if (tris) {
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < n; ++i) {
+            const float* lo = leaves + 6 * i;
+            const float* hi = lo + 3;
+            const float* v = vals + 8 * i;
+            int cs = 0;
+            for (int c = 0; c < 8; ++c) if (v[c] < 0.f) cs |= 1 << c;
+            int64_t o = first[i];
+            for (int t = 0; t < 5 && o < cap; ++t, ++o) {
+                const int* e3 = tri_table + 16 * cs + 3 * t;
+                if (e3[0] == -1) break;
+                for (int q = 0; q < 3; ++q) {
+                    const int ca = edge[2 * e3[q]], cb = edge[2 * e3[q] + 1];
+                    const float va = v[ca], vb = v[cb];
+                    float tc = -va / (vb - va);
+                    if (tc != tc) tc = 0.f;
+                    if (tc > 3.4028234663852886e38f) tc = 3.4028234663852886e38f;
+                    if (tc < -3.4028234663852886e38f) tc = -3.4028234663852886e38f;
+                    tc = fminf(fmaxf(tc, 0.f), 1.f);
+                    for (int k = 0; k < 3; ++k) {
+                        const float pa = vert[3 * ca + k] ? hi[k] : lo[k];
+                        const float pb = vert[3 * cb + k] ? hi[k] : lo[k];
+                        tris[9 * o + 3 * q + k] = (1.f - tc) * pa + tc * pb;
+                    }
+                }
+            }
+        }
+    }
+    free(vals);
+    free(first);
+    return total;
 }

@@ -1,5 +1,6 @@
 """ctypes wrapper of oracle/cpu_tree.c (test infrastructure and CPU baseline only): the
-affine_fixed level-set tree on the host cores with OpenMP."""
+affine_fixed level-set tree and the marching cubes on its leaves on the host cores with
+OpenMP."""
 import ctypes as C
 import os
 import subprocess
@@ -28,12 +29,50 @@ def build(force=False):
 
 def _load():
     lib = C.CDLL(build())
+    lib.cpu_hmc_leaves.restype = C.c_int64
+    lib.cpu_hmc_leaves.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_void_p, C.c_int64,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int64]
     lib.cpu_levelset_tree.restype = C.c_int64
     lib.cpu_levelset_tree.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                       C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_float),
                                       C.POINTER(C.c_float), C.c_int, C.c_float, C.c_int, C.POINTER(C.c_int64),
                                       C.c_void_p, C.c_int64]
     return lib
+
+
+def _net(layers):
+    n = len(layers)
+    A = [np.ascontiguousarray(l[0], np.float32) for l in layers]
+    b = [np.ascontiguousarray(l[1], np.float32) for l in layers]
+    keep = (A, b)
+    return (n, (C.c_int * n)(*[a.shape[0] for a in A]), (C.c_int * n)(*[a.shape[1] for a in A]),
+            (C.c_int * n)(*[ACTS[l[2]] for l in layers]), (C.c_void_p * n)(*[a.ctypes.data for a in A]),
+            (C.c_void_p * n)(*[x.ctypes.data for x in b])), keep
+
+
+def hmc_leaves(layers, leaves, threads=0, want_tris=True):
+    """Marching cubes on every leaf box (leaves (n, 6): lower | upper) as one cell, the
+    n_subcell_depth = 0 extraction of src/kd_tree.py:357-399.  Returns (T, 3, 3) float32
+    triangles in leaf order (or their count when want_tris is False)."""
+    from oracle import mc_table
+    lib = _load()
+    net, keep = _net(layers)
+    leaves = np.ascontiguousarray(leaves, np.float32)
+    table = np.ascontiguousarray(mc_table.make_table(), np.int32)
+    edge = np.ascontiguousarray(mc_table.EDGE, np.int32)
+    vert = np.ascontiguousarray(mc_table.VERT, np.int32)
+    n = leaves.shape[0]
+    count = lib.cpu_hmc_leaves(*net, leaves.ctypes.data, n, table.ctypes.data, edge.ctypes.data, vert.ctypes.data,
+                               int(threads), None, 0)
+    if count < 0:
+        raise ValueError("unsupported network for the C restatement")
+    if not want_tris:
+        return int(count)
+    tris = np.zeros((max(count, 1), 3, 3), np.float32)
+    lib.cpu_hmc_leaves(*net, leaves.ctypes.data, n, table.ctypes.data, edge.ctypes.data, vert.ctypes.data,
+                       int(threads), tris.ctypes.data, count)
+    return tris[:count]
 
 
 def levelset_tree(layers, lower, upper, split_depth, offset=0., threads=0, want_leaves=False):

@@ -7,8 +7,9 @@ numberings alone: for each case the cut edges of every cube face are joined into
 segments (an ambiguous face keeps its inside corners apart), segments chain into
 closed loops, each loop is oriented so its normal points from the inside (value < 0)
 corners to the outside ones, and loops are fan-triangulated from their lowest edge.
-The CUDA library builds the same table in C++ (csrc/mc_table.cuh); tests compare the
-two, and compare this one with the reference's table edge set by edge set.
+The CUDA library builds the same table in C++ (csrc/k_hmc.cu, exported as
+niq_mc_table); tests compare the two, and compare this one case by case with digests
+of the reference's table (tests/golden/mc_digest.npz).
 """
 import numpy as np
 

@@ -162,7 +162,18 @@ def may_contain_bounds(base, aff, err):
     return base - rad, base + rad
 
 
-def truncate_affine(ctx, base, aff, err):
+def _boundary_gap(vals_desc, k, gaps):
+    """Relative gap between the k-th and (k+1)-th largest values (per row of a
+    descending-sorted array), min-folded into ``gaps``: a near tie at the keep/drop
+    boundary makes the kept set, and so the bound, depend on last-ulp rounding."""
+    if gaps is None or vals_desc.shape[1] <= k or k <= 0:
+        return
+    a, b = vals_desc[:, k - 1].astype(np.float64), vals_desc[:, k].astype(np.float64)
+    g = (a - b) / np.maximum(np.abs(a), 1e-30)
+    np.minimum(gaps, g, out=gaps)
+
+
+def truncate_affine(ctx, base, aff, err, gaps=None):
     """src/affine.py:127-162 ('absolute' policy; rows sorted by decreasing L1 magnitude,
     stable, the first ``truncate_count`` kept, the rest folded into ``err``)."""
     if ctx.mode != 'affine_truncate':
@@ -174,13 +185,15 @@ def truncate_affine(ctx, base, aff, err):
         raise RuntimeError("bad policy")
     mags = np.sum(np.abs(aff), axis=-1)                      # (N, rows)
     order = np.argsort(-mags, axis=-1, kind='stable')        # jnp.argsort is stable
+    _boundary_gap(np.take_along_axis(mags, order, axis=-1), n_keep, gaps)
     aff = np.take_along_axis(aff, order[:, :, None], axis=1)
     err = err + np.sum(np.abs(aff[:, n_keep:, :]), axis=1)
     return base, aff[:, :n_keep, :], err
 
 
-def apply_linear_approx(ctx, base, aff, err, alpha, beta, delta):
-    """src/affine.py:164-193."""
+def apply_linear_approx(ctx, base, aff, err, alpha, beta, delta, gaps=None):
+    """src/affine.py:164-193.  ``gaps`` (optional, (N,) float64) collects the relative gap
+    at the truncation / top-k boundary (see _boundary_gap)."""
     base = alpha * base + beta
     aff = alpha[:, None, :] * aff
     delta = np.abs(delta)
@@ -192,12 +205,14 @@ def apply_linear_approx(ctx, base, aff, err, alpha, beta, delta):
         new_aff = np.zeros((n, d, d), dtype=delta.dtype)
         new_aff[:, np.arange(d), np.arange(d)] = delta
         aff = np.concatenate((aff, new_aff), axis=1)
-        base, aff, err = truncate_affine(ctx, base, aff, err)
+        base, aff, err = truncate_affine(ctx, base, aff, err, gaps)
     elif ctx.mode == 'affine_append':
         err = alpha * err
         k = ctx.n_append
         # jax.lax.top_k: descending, ties to the lower index
-        order = np.argsort(-delta, axis=-1, kind='stable')[:, :k]
+        order_all = np.argsort(-delta, axis=-1, kind='stable')
+        _boundary_gap(np.take_along_axis(delta, order_all, axis=-1), k, gaps)
+        order = order_all[:, :k]
         keep_vals = np.take_along_axis(delta, order, axis=-1)
         n, d = delta.shape
         new_aff = np.zeros((n, k, d), dtype=delta.dtype)
@@ -275,7 +290,7 @@ _LINEARIZATIONS = {'relu': _relu_linearization, 'elu': _elu_linearization,
                    'tanh': _tanh_linearization}
 
 
-def affine_forward(params, ctx, base, aff, err, dtype=np.float32):
+def affine_forward(params, ctx, base, aff, err, dtype=np.float32, gaps=None):
     """Walk the spec in affine mode (src/mlp.py:99-111 with apply_func['affine'])."""
     for op in spec_ops(params, dtype):
         name = op[0]
@@ -289,20 +304,20 @@ def affine_forward(params, ctx, base, aff, err, dtype=np.float32):
         elif name in _LINEARIZATIONS:
             lower, upper = may_contain_bounds(base, aff, err)
             alpha, beta, delta = _LINEARIZATIONS[name](lower, upper)
-            base, aff, err = apply_linear_approx(ctx, base, aff, err, alpha, beta, delta)
+            base, aff, err = apply_linear_approx(ctx, base, aff, err, alpha, beta, delta, gaps)
         elif name == 'squeeze_last':            # src/affine_layers.py:164-172
             base, aff, err = base[..., 0], aff[..., 0], err[..., 0]
     return base, aff, err
 
 
-def affine_bounds(params, ctx, center, vecs, dtype=np.float32):
+def affine_bounds(params, ctx, center, vecs, dtype=np.float32, gaps=None):
     """(lower, upper) of the output over general boxes: center (N,3), vecs (N,v,3)."""
     center = np.asarray(center, dtype=dtype)
     vecs = np.asarray(vecs, dtype=dtype)
     ctx = AffineContext(ctx.mode, ctx.truncate_count, ctx.truncate_policy,
                         vecs.shape[1], ctx.n_append)
     base, aff, err = coordinates_in_general_box(ctx, center, vecs)
-    base, aff, err = affine_forward(params, ctx, base, aff, err, dtype)
+    base, aff, err = affine_forward(params, ctx, base, aff, err, dtype, gaps)
     return may_contain_bounds(base, aff, err)
 
 
@@ -354,6 +369,27 @@ def conservative_affine_bounds_model(params, mode, center, vecs, gammas):
     base, aff, err = base[:, 0], aff[:, :, 0], err[:, 0]
     rad = np.abs(aff).sum(1) + err
     return base - rad, base + rad
+
+
+NEAR_REL = 1e-5   # the decision tolerance of the parity rules (relative)
+
+
+def bound_near(lo, hi, offset=0., rel=NEAR_REL):
+    """True where a box's classification (lo > offset, hi < -offset) sits within ``rel``
+    of flipping, relative to the bound's scale max(|lo|, |hi|)."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    scale = np.maximum(np.abs(lo), np.abs(hi)) + 1e-30
+    return (np.abs(lo - offset) <= rel * scale) | (np.abs(hi + offset) <= rel * scale)
+
+
+def value_near(v0, v1, rel=NEAR_REL):
+    """True where the sign test sign(v0) != sign(v1) sits within rounding of flipping:
+    either value within rel of zero, relative to max(|v0|, |v1|, 1)."""
+    v0 = np.abs(np.asarray(v0, np.float64))
+    v1 = np.abs(np.asarray(v1, np.float64))
+    scale = np.maximum(np.maximum(v0, v1), 1.0)
+    return np.minimum(v0, v1) <= rel * scale
 
 
 def sign_from_bounds(lower, upper, offset=0.):
@@ -443,6 +479,18 @@ class OracleFunc:
             return slope_bounds_box(params, center, vecs, self.dtype)
         return affine_bounds(params, self.ctx, center, vecs, self.dtype)
 
+    def bounds_near(self, params, center, vecs, offset=0., rel=NEAR_REL):
+        """Bounds plus a flag per box: True where the classification against ``offset``
+        sits within ``rel`` (relative) of flipping -- a bound within rel * max(|lo|, |hi|)
+        of the threshold, or a near tie at a truncation / top-k boundary -- so that
+        last-ulp differences in the dot products can change it."""
+        gaps = np.full(np.shape(center)[0], np.inf)
+        if self.mode == 'slope_interval':
+            lo, hi = slope_bounds_box(params, center, vecs, self.dtype)
+        else:
+            lo, hi = affine_bounds(params, self.ctx, center, vecs, self.dtype, gaps)
+        return lo, hi, bound_near(lo, hi, offset, rel) | (gaps < rel)
+
     def classify_general_box(self, params, center, vecs, offset=0.):
         lo, hi = self.bounds_general(params, center, vecs)
         return sign_from_bounds(lo, hi, offset)
@@ -501,9 +549,17 @@ def get_default_cast_opts():
             'interval_init_size': 0.1, 'refine_width_fac': 2., 'n_side_init': 16}
 
 
-def cast_rays(funcs, params_list, roots, dirs, opts):
+def cast_rays(funcs, params_list, roots, dirs, opts, trace=False):
     """src/queries.py:39-175.  Each ray steps independently; the bucketing only changes
-    ``N_evals``, which is reproduced by replaying the bucket sizes."""
+    ``N_evals``, which is reproduced by replaying the bucket sizes.
+
+    With ``trace`` a fifth array is returned: per ray, the step index (the ray's count
+    when the decision was taken) of its first near-threshold decision -- a segment bound
+    within NEAR_REL of its sign threshold or a hit test with a value within NEAR_REL of
+    zero (see bounds_near, value_near) -- or a huge value when it took none.  Two
+    implementations that differ only by rounding can send a ray down different paths
+    only from such a decision, so their results for the ray may differ only when
+    first_near < min(count_a, count_b)."""
     f32 = funcs[0].dtype
     roots = np.asarray(roots, f32)
     dirs = np.asarray(dirs, f32)
@@ -519,24 +575,35 @@ def cast_rays(funcs, params_list, roots, dirs, opts):
     bucket = N
     n_evals = 0
     n_sub = opts['n_substeps']
+    first_near = np.full(N, np.iinfo(np.int32).max, np.int64)
     while True:
         r, d = roots[active], dirs[active]
         tt, ss = t[active], step[active]
         is_hit = np.zeros(active.shape[0], bool)
         hit_id = np.zeros(active.shape[0], np.int32)
         n_inner = np.zeros(active.shape[0], np.int32)
-        for _ in range(n_sub):                              # src/queries.py:44-92
+        for i_sub in range(n_sub):                          # src/queries.py:44-92
             can_step = ~is_hit
+            live = ~is_hit
             n_inner += (~is_hit).astype(np.int32)
             for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
                 pos_start = r + tt[:, None] * d
                 half_vec = 0.5 * ss[:, None] * d
                 pos_mid = pos_start + half_vec
-                btype = func.classify_general_box(params, pos_mid, half_vec[:, None, :])
+                if trace:
+                    lo, hi, near = func.bounds_near(params, pos_mid, half_vec[:, None, :])
+                    btype = sign_from_bounds(lo, hi)
+                else:
+                    btype = func.classify_general_box(params, pos_mid, half_vec[:, None, :])
                 can_step &= (btype == SIGN_POSITIVE) | (btype == SIGN_NEGATIVE)
                 pos_eps = r + (tt + np.asarray(hit_eps, f32))[:, None] * d
                 v0 = func(params, pos_start)
                 v1 = func(params, pos_eps)
+                if trace:
+                    near = live & (near | value_near(v0, v1))
+                    step_idx = count[active] + i_sub
+                    idx = active[near]
+                    first_near[idx] = np.minimum(first_near[idx], step_idx[near])
                 this_hit = np.sign(v0) != np.sign(v1)
                 hit_id = np.where(this_hit, fid, hit_id).astype(np.int32)
                 is_hit |= this_hit
@@ -560,6 +627,8 @@ def cast_rays(funcs, params_list, roots, dirs, opts):
             break
         if fits_in_smaller_bucket(n_valid, bucket):
             bucket = get_next_bucket_size(n_valid)
+    if trace:
+        return out_t, out_hit, out_count, n_evals, first_near
     return out_t, out_hit, out_count, n_evals
 
 
@@ -1035,8 +1104,17 @@ def find_any_intersection(funcs, params_list, lower, upper, eps, max_rounds=200)
 # Closest point  (src/kd_tree.py:659-802)
 # ----------------------------------------------------------------------------------------
 
-def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048):
-    """src/kd_tree.py:659-802 with the same global LIFO stack and batch pops."""
+def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_process_size=2048, trace=False):
+    """src/kd_tree.py:659-802 with the same global LIFO stack and batch pops.
+
+    With ``trace`` a third value is returned, a dict: ``near`` (Q,) bool, True for a
+    query one of whose node decisions sat within NEAR_REL of flipping (the box
+    classification, a sample's sign, or the pruning comparison cdist < best);
+    ``first_near_round``, the first round in which any query took such a decision; and
+    ``last_round`` (Q,), the last round that processed a node of the query.  All
+    queries share one stack, so after the first near decision the batches of two
+    implementations may hold different nodes; a query can then differ between them only
+    if it is ``near`` itself or still had nodes processed at or after that round."""
     dt = func.dtype
     q = np.asarray(query_points, dt)
     Q = q.shape[0]
@@ -1050,6 +1128,9 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
     eps_w = np.asarray(eps / np.sqrt(np.asarray(3., dt)), dt)
     offs = _sample_offsets().astype(dt)
     rounds = 0
+    near_q = np.zeros(Q, bool)
+    last_round = np.full(Q, -1, np.int64)
+    first_near_round = None
     while top > 0:
         pop = max(top - B, 0)
         lo, hi, ids = st_lo[pop:top], st_hi[pop:top], st_id[pop:top]
@@ -1063,12 +1144,29 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
         max_d = cdist + diag
         small = width < eps_w
         pts = center[:, None, :] + (hi - lo)[:, None, :] * offs[None, :, :]
-        types = func.classify_box(params, lo, hi)
+        if trace:
+            c_ = 0.5 * (lo + hi)
+            v_ = np.zeros((n, 3, 3), dt)
+            v_[:, np.arange(3), np.arange(3)] = hi - c_
+            blo, bhi, near = func.bounds_near(params, c_, v_)
+            types = sign_from_bounds(blo, bhi)
+        else:
+            types = func.classify_box(params, lo, hi)
         outside = (types == SIGN_NEGATIVE) | (types == SIGN_POSITIVE)
         sv = func(params, pts.reshape(-1, 3)).reshape(n, 7)
         spans = ~(np.all(sv < 0, axis=1) | np.all(sv > 0, axis=1))
         this_d = np.where(spans, max_d, np.inf).astype(dt)
         needs = (~outside) & (~small) & (cdist < qmd)
+        if trace:
+            svn = np.abs(sv.astype(np.float64))
+            near |= np.any(svn <= NEAR_REL * np.maximum(svn.max(axis=1, keepdims=True), 1.0), axis=1)
+            fin = np.isfinite(qmd)
+            near |= fin & (np.abs(cdist.astype(np.float64) - qmd) <=
+                           NEAR_REL * np.maximum(cdist, np.where(fin, qmd, 0)).astype(np.float64))
+            near_q[ids[near]] = True
+            last_round[ids] = rounds
+            if first_near_round is None and near.any():
+                first_near_round = rounds
         np.minimum.at(min_dist, ids, this_d)
         newmin = this_d == min_dist[ids]
         min_loc[ids[newmin]] = center[newmin]   # scatter-set; the last duplicate wins
@@ -1082,4 +1180,8 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
         st_id = np.concatenate((st_id[:pop], new_id))
         top = pop + 2 * m
         rounds += 1
+    if trace:
+        return min_dist, min_loc, {'near': near_q, 'last_round': last_round,
+                                   'first_near_round': np.iinfo(np.int64).max if first_near_round is None
+                                   else first_near_round}
     return min_dist, min_loc

@@ -1,6 +1,8 @@
 """Generate the golden vectors in this folder by running the reference's own code.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <path of the reference checkout> [--only NAME]
+
+(or set NIQ_REFERENCE to that path).
 
 The reference (nmwsharp/neural-implicit-queries) is pure JAX and JAX is not installed
 here, so its ``src/*.py`` modules are imported unchanged over the NumPy stand-in in
@@ -52,9 +54,13 @@ def rand_boxes(rng, n, v):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default='/root/reference')
-    ap.add_argument('--only', default=None, help='write one fixture only (e.g. frustum)')
+    ap.add_argument('--reference', default=os.environ.get('NIQ_REFERENCE'),
+                    help='root of the reference checkout (default: $NIQ_REFERENCE)')
+    ap.add_argument('--only', default=None,
+                    help='write one fixture only: frustum, camera, mc, samples')
     args = ap.parse_args()
+    if not args.reference or not os.path.isdir(os.path.join(args.reference, 'src')):
+        ap.error('--reference (or NIQ_REFERENCE) must name the reference checkout')
     jax_standin.install()
     sys.path.insert(0, os.path.join(args.reference, 'src'))
     import jax.numpy as jnp
@@ -75,6 +81,15 @@ def main():
     t0 = time.time()
     if args.only == 'frustum':
         frustum_fixture(queries, load_as_reference, models, t0)
+        return
+    if args.only == 'camera':
+        camera_fixture()
+        return
+    if args.only == 'mc':
+        mc_fixture(extract_cell)
+        return
+    if args.only == 'samples':
+        samples_fixture(args.reference, affine, slope_interval, queries, kd_tree, load_as_reference, t0)
         return
 
     # ---------------------------------------------------------------- point evals + bounds
@@ -238,6 +253,108 @@ def frustum_fixture(queries, load_as_reference, models, t0):
         print(f'frustum {name} {time.time() - t0:.1f}s', flush=True)
     out['frustum/cam'] = np.concatenate([eye, look, up, left, [40., 30., 12, 10]]).astype(np.float32)
     np.savez_compressed(os.path.join(HERE, 'frustum.npz'), **out)
+
+
+def camera_fixture():
+    """render.generate_camera_rays and render.look_at (src/render.py:17-50,229-242): the
+    default plain-method camera (eye at distance 3 on +z, 60 degree field of view) at
+    three resolutions, and look_at for a few eyes and both up axes."""
+    import render
+    import jax.numpy as jnp
+    out = {}
+    eyes = np.array([[0., 0., 3.], [1.5, 2., -2.1], [-2.5, 0.3, 1.2], [0.2, -3., 0.4]], np.float32)
+    out['look_at/eyes'] = eyes
+    for up in ('y', 'z'):
+        res = [tuple(np.asarray(x) for x in render.look_at(jnp.array(e), up_dir=up)) for e in eyes]
+        for j, name in enumerate(('look', 'up', 'left')):
+            out[f'look_at/{up}/{name}'] = np.stack([r[j] for r in res]).astype(np.float32)
+    look, up, _ = (np.asarray(x) for x in render.look_at(jnp.array(eyes[0])))
+    for res_, fov in ((5, 60.), (33, 60.), (128, 60.), (16, 35.)):
+        e = eyes[0] if fov == 60. else eyes[1]
+        lk, u, _ = (np.asarray(x) for x in render.look_at(jnp.array(e)))
+        roots, dirs = render.generate_camera_rays(jnp.array(e), jnp.array(lk), jnp.array(u), res=res_, fov_deg=fov)
+        out[f'cam/{res_}/eye'], out[f'cam/{res_}/look'], out[f'cam/{res_}/up'] = e, lk, u
+        out[f'cam/{res_}/fov'] = np.float32(fov)
+        out[f'cam/{res_}/roots'], out[f'cam/{res_}/dirs'] = np.asarray(roots), np.asarray(dirs)
+    np.savez_compressed(os.path.join(HERE, 'camera.npz'), **out)
+    print('camera done', flush=True)
+
+
+def mc_fixture(extract_cell):
+    """Per-case digests of the reference's marching-cubes table (src/extract_cell.py:12-268)
+    in the triangulation-independent canonical form of mc_canon.py: the tests pin this
+    project's generated table against them without the table itself being committed."""
+    import mc_canon
+    from oracle import mc_table
+    ref = np.asarray(extract_cell.MC_TRI_TABLE_RAW)
+    out = {'mc/digest': mc_canon.case_digests(ref, mc_table.VERT, mc_table.EDGE)}
+    np.savez_compressed(os.path.join(HERE, 'mc_digest.npz'), **out)
+    print('mc digests done', flush=True)
+
+
+SAMPLE_MODELS = ('fox', 'hammer', 'bunny', 'birdcage_occ')
+
+
+def samples_fixture(reference, affine, slope_interval, queries, kd_tree, load_as_reference, t0):
+    """The reference's own sample models (sample_inputs/*.npz: ReLU 3->32x8, ReLU 3->64x8,
+    ELU 3->64x8, ReLU 3->64x8): their parameters go to sample_models.npz, the reference's
+    outputs on them to samples.npz -- point values, box bounds in four modes, the
+    level-set tree (12 bisections) and a small ray cast."""
+    import jax.numpy as jnp
+    params_out, out = {}, {}
+    rng = np.random.default_rng(4321)
+    mode_kw = {'interval': {}, 'affine_fixed': {}, 'slope_interval': {},
+               'affine_truncate': {'affine_n_truncate': 8, 'affine_truncate_policy': 'absolute'}}
+    eye = np.array([0., 0., 3.], np.float32)
+    import render
+    look, up, _ = (np.asarray(x) for x in render.look_at(jnp.array(eye)))
+    roots, dirs = (np.asarray(a) for a in render.generate_camera_rays(jnp.array(eye), jnp.array(look),
+                                                                        jnp.array(up), res=12, fov_deg=60.))
+    out['rays/roots'], out['rays/dirs'] = roots, dirs
+    lower, upper = jnp.array((-1., -1., -1.)), jnp.array((1., 1., 1.))
+    for name in SAMPLE_MODELS:
+        src = dict(np.load(os.path.join(reference, 'sample_inputs', name + '.npz')))
+        params_out.update(flat(f'model/{name}', src))
+        pts = rng.uniform(-1.1, 1.1, (64, 3)).astype(np.float32)
+        f, p = load_as_reference(src, name, 'affine_fixed')
+        out[f'{name}/points/x'] = pts
+        out[f'{name}/points/f'] = np.asarray(jax_standin._vmap(lambda x: f(p, x))(pts))
+        center, vecs = rand_boxes(rng, 32, 3)
+        out[f'{name}/boxes/center'], out[f'{name}/boxes/vecs'] = center, vecs
+        for mode, kw in mode_kw.items():
+            f, p = load_as_reference(src, name, mode, **kw)
+            if mode == 'slope_interval':
+                def bounds_one(c, vv):
+                    inp = slope_interval.coordinates_in_general_box(c, vv)
+                    o = f.slope_interval_func(p, inp)
+                    sl, su = slope_interval.slope_bounds(o)
+                    return slope_interval.primal_may_contain_bounds(o, sl, su)
+            else:
+                def bounds_one(c, vv):
+                    ctx = dataclasses.replace(f.ctx, affine_domain_terms=vv.shape[0])
+                    inp = affine.coordinates_in_general_box(ctx, c, vv)
+                    o = f.affine_func(p, inp, {'ctx': ctx})
+                    return affine.may_contain_bounds(ctx, o)
+            lo, hi = jax_standin._vmap(bounds_one)(center, vecs)
+            out[f'{name}/boxes/{mode}/lower'], out[f'{name}/boxes/{mode}/upper'] = np.asarray(lo), np.asarray(hi)
+        print(f'{name} bounds {time.time() - t0:.1f}s', flush=True)
+        f, p = load_as_reference(src, name, 'affine_fixed')
+        d = kd_tree.construct_uniform_unknown_levelset_tree(f, p, lower, upper, split_depth=12,
+                                                            with_interior_nodes=True,
+                                                            with_exterior_nodes=True, offset=0.)
+        for kind in ('unknown', 'interior', 'exterior'):
+            valid = np.asarray(d[f'{kind}_node_valid'])
+            out[f'{name}/tree/{kind}/lower'] = np.asarray(d[f'{kind}_node_lower'])[valid]
+            out[f'{name}/tree/{kind}/upper'] = np.asarray(d[f'{kind}_node_upper'])[valid]
+        print(f'{name} tree {time.time() - t0:.1f}s', flush=True)
+        opts = queries.get_default_cast_opts()
+        opts['n_max_step'] = 48
+        t, hid, cnt, nev = queries.cast_rays((f,), (p,), jnp.array(roots), jnp.array(dirs), opts)
+        out[f'{name}/rays/t'], out[f'{name}/rays/hit_id'] = np.asarray(t), np.asarray(hid)
+        out[f'{name}/rays/count'] = np.asarray(cnt)
+        print(f'{name} rays {time.time() - t0:.1f}s', flush=True)
+    np.savez_compressed(os.path.join(HERE, 'sample_models.npz'), **params_out)
+    np.savez_compressed(os.path.join(HERE, 'samples.npz'), **out)
 
 
 def _camera(eye, look, up, res, fov):

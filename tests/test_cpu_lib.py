@@ -5,7 +5,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import GOLDEN, ROOT, golden
 
 
 @pytest.fixture(scope='module')
@@ -42,35 +42,39 @@ def test_mc_table_library_matches_oracle(lib):
 
 
 def test_mc_table_equivalent_to_reference():
-    """Same polygons (edge sets per connected piece) and orientation as the reference's
-    third-party table, case by case."""
+    """Same polygons (edge sets per connected piece) and orientation (vector area, which
+    does not depend on the triangulation) as the reference's third-party table, case by
+    case: the digests in mc_digest.npz were computed from the reference's table by
+    tests/golden/make_golden.py."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import mc_canon
     from oracle import mc_table
-    from test_oracle_golden import reference_mc_table
-    ref = reference_mc_table()
-    T = mc_table.make_table()
-    mid = (mc_table.VERT[mc_table.EDGE[:, 0]] + mc_table.VERT[mc_table.EDGE[:, 1]]) / 2.0
+    ref = golden('mc_digest.npz')['mc/digest']
+    ours = mc_canon.case_digests(mc_table.make_table(), mc_table.VERT, mc_table.EDGE)
+    bad = np.nonzero(ref != ours)[0]
+    assert bad.size == 0, f'cases differing from the reference table: {bad.tolist()}'
 
-    def tris(row):
-        return [tuple(row[i:i + 3]) for i in range(0, 15, 3) if row[i] != -1]
 
-    def comps(ts):
-        groups = []
-        for t in ts:
-            hit = [g for g in groups if set(t) & {x for tt in g for x in tt}]
-            groups = [g for g in groups if g not in hit] + [[t] + [tt for g in hit for tt in g]]
-        return groups
-
-    def vec_area(g):
-        return sum(np.cross(mid[b] - mid[a], mid[c] - mid[a]) for a, b, c in g)
-
-    for c in range(256):
-        gr, gm = comps(tris(ref[c])), comps(tris(T[c]))
-        assert sorted(sorted({x for t in g for x in t}) for g in gr) == \
-            sorted(sorted({x for t in g for x in t}) for g in gm), c
-        for g in gr:
-            es = {x for t in g for x in t}
-            h = [x for x in gm if {y for t in x for y in t} == es][0]
-            assert np.dot(vec_area(g), vec_area(h)) > 0, c
+def test_camera_rays_golden(niq):
+    """render.generate_camera_rays / look_at bit for bit against the reference's own
+    functions (src/render.py:17-50,229-242) run over the NumPy stand-in."""
+    g = golden('camera.npz')
+    R = niq.render
+    eyes = g['look_at/eyes']
+    for up in ('y', 'z'):
+        for i, e in enumerate(eyes):
+            with np.errstate(invalid='ignore'):
+                got = R.look_at(e, up_dir=up)
+            for j, name in enumerate(('look', 'up', 'left')):
+                np.testing.assert_array_equal(got[j], g[f'look_at/{up}/{name}'][i])
+    for res in (5, 33, 128, 16):
+        k = f'cam/{res}/'
+        roots, dirs = R.generate_camera_rays(g[k + 'eye'], g[k + 'look'], g[k + 'up'], res=res,
+                                             fov_deg=float(g[k + 'fov']))
+        assert roots.dtype == np.float32 and dirs.dtype == np.float32
+        np.testing.assert_array_equal(roots, g[k + 'roots'])
+        np.testing.assert_array_equal(dirs, g[k + 'dirs'])
 
 
 def test_pack_roundtrip_and_errors(niq):

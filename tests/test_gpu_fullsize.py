@@ -66,3 +66,22 @@ def test_rays_1024_persistent_equals_plain(niq, gpu_ready):
     for x, y in zip(a[:3], b[:3]):
         np.testing.assert_array_equal(x, y)
     assert (a[1] > 0).sum() > 500000
+
+
+def test_tree_24_bisections_matches_c_oracle(niq, gpu_ready):
+    """The level-set tree of the 12-sphere model to 24 bisections (256^3 leaves) in the
+    reference's arithmetic (conservative=False) against the oracle's C restatement
+    (oracle/cpu_tree.c) at the same size: identical leaf sets except boxes whose path
+    from the root holds a decision within rounding of its threshold (tests/parity.py)."""
+    from oracle import cpu_tree
+    from parity import box_set_diff, unexplained_boxes
+    params = niq.workloads.spheres_sdf_model()
+    f = _func(niq, params, conservative=False)
+    lo, hi = -np.ones(3, np.float32), np.ones(3, np.float32)
+    d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, lo, hi, split_depth=24)
+    n, nb, leaves = cpu_tree.levelset_tree(niq.mlp.spec_layers(params), lo, hi, 24, want_leaves=True)
+    assert n == leaves.shape[0] > 500000
+    extra, missing = box_set_diff(d['unknown_node_lower'], d['unknown_node_upper'], leaves[:, :3], leaves[:, 3:])
+    print(f'24-bisection tree: {len(extra)} extra, {len(missing)} missing of {n} leaves')
+    bad = unexplained_boxes(params, np.concatenate([extra, missing]), lo, hi)
+    assert len(bad) == 0, bad[:5]

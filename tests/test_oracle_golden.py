@@ -3,6 +3,7 @@ reference's own source (tests/golden/make_golden.py)."""
 import numpy as np
 import pytest
 
+from parity import ray_match, unexplained_rays
 from conftest import golden, model_from
 
 MODES = {'interval': {}, 'affine_fixed': {}, 'affine_all': {},
@@ -69,13 +70,12 @@ def test_cast_rays(R, gr, mode):
     f = R.generate_implicit(params, mode)
     opts = R.get_default_cast_opts()
     opts['n_max_step'] = 64
-    t, hid, cnt, nev = R.cast_rays([f], [params], gr['rays/roots'], gr['rays/dirs'], opts)
+    t, hid, cnt, nev, near = R.cast_rays([f], [params], gr['rays/roots'], gr['rays/dirs'], opts, trace=True)
     gt, ghid, gcnt = gr[f'rays/{mode}/t'], gr[f'rays/{mode}/hit_id'], gr[f'rays/{mode}/count']
-    same = (hid == ghid) & (cnt == gcnt) & np.isclose(t, gt, rtol=1e-4, atol=1e-5)
-    # rays are chaotic in their classify decisions; all but a handful must agree exactly
-    assert same.mean() >= 0.97, same.mean()
-    assert np.all(np.isclose(t[hid > 0], gt[hid > 0], atol=2e-2) | ~(ghid[hid > 0] > 0))
-    assert int(nev) == int(gr[f'rays/{mode}/n_evals']) or not same.all()
+    # a ray may differ from the reference only after a decision within rounding of its
+    # threshold (tests/parity.py)
+    assert unexplained_rays(t, hid, cnt, gt, ghid, gcnt, near).size == 0
+    assert int(nev) == int(gr[f'rays/{mode}/n_evals']) or not ray_match(t, hid, cnt, gt, ghid, gcnt).all()
 
 
 def test_cast_rays_two_functions_substeps(R, gr):
@@ -86,9 +86,9 @@ def test_cast_rays_two_functions_substeps(R, gr):
     opts['n_max_step'] = 48
     opts['n_substeps'] = 2
     sub = slice(0, gr['rays/roots'].shape[0], 3)
-    t, hid, cnt, nev = R.cast_rays([f, f], [p1, p2], gr['rays/roots'][sub], gr['rays/dirs'][sub], opts)
-    same = (hid == gr['rays2/hit_id']) & (cnt == gr['rays2/count']) & np.isclose(t, gr['rays2/t'], rtol=1e-4, atol=1e-5)
-    assert same.mean() >= 0.97
+    t, hid, cnt, nev, near = R.cast_rays([f, f], [p1, p2], gr['rays/roots'][sub], gr['rays/dirs'][sub], opts,
+                                         trace=True)
+    assert unexplained_rays(t, hid, cnt, gr['rays2/t'], gr['rays2/hit_id'], gr['rays2/count'], near).size == 0
 
 
 def _sorted_boxes(lo, hi):
@@ -122,19 +122,6 @@ def test_levelset_tree_thresh(R, gt_):
                                                   offset=0.05, batch_process_size=128)
     np.testing.assert_array_equal(d['unknown_node_lower'], gt_['tree_thresh/lower'])
     np.testing.assert_array_equal(d['unknown_node_upper'], gt_['tree_thresh/upper'])
-
-
-def reference_mc_table():
-    """The reference's triangle table, read from its source file at test time."""
-    import ast
-    import os
-    path = '/root/reference/src/extract_cell.py'
-    if not os.path.exists(path):
-        pytest.skip('reference tree not present')
-    src = open(path).read()
-    start = src.index('MC_TRI_TABLE_RAW = [')
-    end = src.index(']]', start) + 2
-    return np.array(ast.literal_eval(src[start + len('MC_TRI_TABLE_RAW = '):end]))
 
 
 @pytest.mark.parametrize('name', ['one', 'two'])
@@ -172,3 +159,61 @@ def test_c_restatement_matches_numpy_oracle(R):
     ref = np.concatenate([d['unknown_node_lower'], d['unknown_node_upper']], 1)
     assert n == ref.shape[0] and nb == d['n_boxes_classified']
     np.testing.assert_array_equal(leaves, ref)
+
+
+SAMPLE_NAMES = ('fox', 'hammer', 'bunny', 'birdcage_occ')
+SAMPLE_MODES = {'interval': {}, 'affine_fixed': {}, 'slope_interval': {},
+                'affine_truncate': {'affine_n_truncate': 8}}
+
+
+@pytest.fixture(scope='module')
+def gs_():
+    return golden('samples.npz'), golden('sample_models.npz')
+
+
+@pytest.mark.parametrize('name', SAMPLE_NAMES)
+def test_sample_models_oracle(R, gs_, name):
+    """The oracle against the reference's outputs on its own sample models: point values,
+    bounds in four modes, the 12-bisection level-set tree (same boxes in the same order)
+    and a 12 x 12 ray cast."""
+    g, m = gs_
+    params = model_from(m, f'model/{name}')
+    np.testing.assert_allclose(R.eval_points(params, g[f'{name}/points/x']), g[f'{name}/points/f'],
+                               rtol=1e-5, atol=1e-6)
+    c, vv = g[f'{name}/boxes/center'], g[f'{name}/boxes/vecs']
+    for mode, kw in SAMPLE_MODES.items():
+        f = R.generate_implicit(params, mode, **kw)
+        lo, hi = f.bounds_general(params, c, vv)
+        glo, ghi = g[f'{name}/boxes/{mode}/lower'], g[f'{name}/boxes/{mode}/upper']
+        scale = np.maximum(np.abs(glo), np.abs(ghi)) + 1e-3
+        assert np.max(np.abs(lo - glo) / scale) <= 1e-5 and np.max(np.abs(hi - ghi) / scale) <= 1e-5, mode
+    f = R.generate_implicit(params, 'affine_fixed')
+    d = R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=12,
+                                                  with_interior_nodes=True, with_exterior_nodes=True)
+    for kind in ('unknown', 'interior', 'exterior'):
+        np.testing.assert_array_equal(d[f'{kind}_node_lower'], g[f'{name}/tree/{kind}/lower'])
+        np.testing.assert_array_equal(d[f'{kind}_node_upper'], g[f'{name}/tree/{kind}/upper'])
+    opts = R.get_default_cast_opts()
+    opts['n_max_step'] = 48
+    t, hid, cnt, _, near = R.cast_rays([f], [params], g['rays/roots'], g['rays/dirs'], opts, trace=True)
+    assert unexplained_rays(t, hid, cnt, g[f'{name}/rays/t'], g[f'{name}/rays/hit_id'], g[f'{name}/rays/count'],
+                            near).size == 0
+
+
+def test_c_marching_cubes_matches_numpy_oracle(R):
+    """oracle/cpu_tree.c's marching cubes on the leaves (n_subcell_depth 0, the CPU
+    baseline's second phase) gives the NumPy oracle's triangles, in the same order, to
+    fp32 rounding of the point values."""
+    from oracle import cpu_tree, mc_table
+    import importlib
+    niq = importlib.import_module('neural-implicit-queries_gb300')
+    params = niq.workloads.spheres_sdf_model()
+    layers = niq.mlp.spec_layers(params)
+    _, _, leaves = cpu_tree.levelset_tree(layers, -np.ones(3), np.ones(3), 12, want_leaves=True)
+    tris = cpu_tree.hmc_leaves(layers, leaves)
+    o = R.generate_implicit(params, 'affine_fixed')
+    ref = R.hierarchical_marching_cubes(o, params, -np.ones(3), np.ones(3), 4,
+                                        (mc_table.make_table(), mc_table.EDGE, mc_table.VERT), n_subcell_depth=0)
+    assert tris.shape == ref.shape and tris.shape[0] > 500
+    np.testing.assert_allclose(tris, ref, atol=1e-5)
+    assert cpu_tree.hmc_leaves(layers, leaves, want_tris=False) == tris.shape[0]
