@@ -277,9 +277,8 @@ def run_ours(args):
         "roofline": {"bound": "fp32", "kernel": "k_tree (persistent level-set tree)",
                      "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak,
-                     # DRAM bytes of one k_tree launch: the ncu capture of the 18-bisection tree
-                     # (profiles/k_tree_spheres64_split18_full.md: 148.5 KB read + 6.9 KB
-                     # written for 332,953 boxes) scaled by boxes to this launch
+                     # DRAM bytes of one k_tree launch: an ncu capture of the 18-bisection tree
+                     # (148.5 KB read + 6.9 KB written for 332,953 boxes) scaled by boxes
                      "traffic": (148480 + 6912) / 332953 * n_boxes,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the "
                                        "18-bisection tree, scaled to this launch's boxes; the level arrays stay in L2",

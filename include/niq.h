@@ -253,15 +253,17 @@ int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts,
  * has no allocation-free path).
  * - No device memory is allocated, by this call or by a model handle: the caller passes
  *   the packed spec twice, a host copy (validated and used for launch planning) and a
- *   16-byte-aligned device copy that the kernels read.
+ *   16-byte-aligned device copy that the kernels read.  The two must hold the same
+ *   bytes; the call compares their headers and fails with NIQ_ERR_BAD_SPEC otherwise.
  * - Scratch (level counters and two level buffers) is a static device array of the
  *   library, NIQ_STATIC_TREE_NODES nodes per level (about 3 MB), which every GPU that
  *   loads the library holds until the process exits.  A level, or a result list, larger
  *   than NIQ_STATIC_TREE_NODES nodes fails with NIQ_ERR_CAPACITY.
  * - Results go to the caller's arrays, each (NIQ_STATIC_TREE_NODES, 3) float32 (interior
  *   and exterior only when requested in flags); counts_out as for niq_levelset_tree.
- * - The first call on a device looks up the scratch array's device address; make that
- *   first call before any stream capture.  Every call clears the counters it needs.
+ * - The first call on a device looks up the scratch array's device address and keeps it
+ *   for the process; make that first call before any stream capture, and make no call
+ *   after a cudaDeviceReset of that device.  Every call clears the counters it needs.
  * - All calls share the one scratch array: calls that overlap on the GPU (two streams,
  *   or two host threads) race and corrupt each other's results.  Syncs the stream. */
 #define NIQ_STATIC_TREE_NODES 65536

@@ -415,7 +415,9 @@ static __device__ __align__(256) unsigned char g_static_tree_scratch[kStaticTree
 static void* g_static_tree_ptr[64] = {nullptr};
 static std::mutex g_static_tree_mu;
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array on the current device, looked up once per device
+// (the first call on it) and kept for the process: after cudaDeviceReset the address is
+// stale, so no call may follow a device reset.
 static int static_tree_scratch(void** out) {
     int dev = 0;
     NIQ_CUDA(cudaGetDevice(&dev));
@@ -477,6 +479,17 @@ extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void
     rc = static_tree_scratch(&scratch);
     if (rc) return rc;
     cudaStream_t s = as_stream(stream);
+    // Launch planning (threads per item, shared-memory size, resident weights) uses the
+    // host copy while the kernel stages weights by the device copy's header: the two
+    // headers must be the same bytes, or the kernel would write past the shared memory
+    // it was planned for.  A stack copy of the device header, no allocation.
+    {
+        NiqSpecHeader Hd;
+        NIQ_CUDA(cudaMemcpyAsync(&Hd, packed_spec_device, sizeof(Hd), cudaMemcpyDeviceToHost, s));
+        NIQ_CUDA(cudaStreamSynchronize(s));
+        NIQ_REQUIRE(memcmp(&Hd, &H, sizeof(H)) == 0, NIQ_ERR_BAD_SPEC,
+                    "the device copy of the spec has another header than the host copy");
+    }
     char* base = reinterpret_cast<char*>(scratch);
     TreeWs* ws = reinterpret_cast<TreeWs*>(base);
     TreeBufs B;

@@ -170,6 +170,8 @@ def _boundary_gap(vals_desc, k, gaps):
         return
     a, b = vals_desc[:, k - 1].astype(np.float64), vals_desc[:, k].astype(np.float64)
     g = (a - b) / np.maximum(np.abs(a), 1e-30)
+    # a tie between zero magnitudes keeps or drops nothing: not a decision
+    g = np.where(a > 0, g, np.inf)
     np.minimum(gaps, g, out=gaps)
 
 

@@ -82,3 +82,27 @@ def test_static_tree_rejects_levels_beyond_the_scratch(niq, gpu_ready):
                                       counts.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == L.NIQ_ERR_CAPACITY
     assert b'static scratch' in lib.niq_last_error()
+
+
+def test_static_tree_rejects_a_device_spec_unlike_the_host_spec(niq, gpu_ready):
+    """Launch planning reads the host copy of the spec, the kernel the device copy: a
+    device copy with another header is refused before any launch, and the next call with
+    matching copies still succeeds."""
+    import torch
+    L = importlib.import_module('neural-implicit-queries_gb300._lib')
+    lib = L.load()
+    params = niq.workloads.spheres_sdf_model()
+    blob = niq.mlp.pack(params)
+    other = niq.mlp.pack(niq.workloads.he_mlp([3, 32, 32, 1], 'relu', seed=4, grid=8))
+    opts = L.bound_opts('affine_fixed', conservative=True)
+    lo3, hi3 = (C.c_float * 3)(-1., -1., -1.), (C.c_float * 3)(1., 1., 1.)
+    outs = [torch.empty((STATIC_NODES, 3), dtype=torch.float32, device='cuda') for _ in range(2)]
+    counts = torch.zeros(4, dtype=torch.int64, device='cuda')
+    stream = torch.cuda.current_stream().cuda_stream
+    for dev, want in ((other, L.NIQ_ERR_BAD_SPEC), (blob, 0)):
+        dev_blob = torch.frombuffer(bytearray(dev), dtype=torch.uint8).cuda()
+        rc = lib.niq_levelset_tree_static(blob, dev_blob.data_ptr(), len(blob), C.byref(opts), lo3, hi3, 8, 0, 0.0, 0,
+                                          outs[0].data_ptr(), outs[1].data_ptr(), None, None, None, None,
+                                          counts.data_ptr(), stream)
+        assert rc == want, lib.niq_last_error()
+    assert int(counts[0]) > 0
