@@ -107,6 +107,14 @@ int niq_version(void);
 #define NIQ_TUNE_BATCHED_CHUNK        0
 #define NIQ_TUNE_BATCHED_CTAS_PER_SM  1
 #define NIQ_TUNE_TREE_CTAS_PER_SM     2
+/* Limits of the bounded device-side waits, as 1 + the number of polls a wait may make
+ * before it gives up with NIQ_ERR_TIMEOUT (0 = the built-in limit: 2^28 polls of a grid
+ * barrier, 2^24 of an mbarrier on tensor-core work; 1 = give up at once).  The waits are
+ * those of the persistent tree and intersection kernels (grid barrier between levels)
+ * and of the tensor-core kernels (completion of their MMAs; a kernel that gave up still
+ * waits for its MMAs with the built-in limit before it releases tensor memory). */
+#define NIQ_TUNE_BARRIER_POLLS        3
+#define NIQ_TUNE_MBAR_POLLS           4
 int niq_tune_set(int32_t param, int32_t value);
 int niq_tune_get(int32_t param, int32_t* value);
 /* Number of SMs and resident-CTA counts of the current device (for workspace sizing). */
@@ -282,6 +290,29 @@ int niq_levelset_tree_batches(const niq_model* model, const niq_bound_opts* opts
                               const float* upper, int32_t split_depth, int64_t node_terminate_thresh, float offset,
                               int32_t flags, int64_t batch_process_size, int64_t node_capacity,
                               int64_t* counts_out, void* workspace, size_t workspace_bytes, void* stream);
+/* The tree in every mode, including the growing-term ones (affine_truncate,
+ * affine_append, affine_all), which the kernels above reject: the reference's level loop
+ * (src/kd_tree.py:137-198) with each level classified by niq_classify_boxes in chunks of
+ * 65,536 nodes and the results and children appended on the device; one host read of
+ * the level size per level.  Syncs.  Its workspace (niq_tree_growing_workspace_size) has
+ * the layout of niq_tree_workspace_size's followed by the chunk scratch, so
+ * niq_tree_result reads its nodes. */
+size_t niq_tree_growing_workspace_size(const niq_model* model, const niq_bound_opts* opts, int64_t node_capacity,
+                                       int32_t flags);
+int niq_levelset_tree_growing(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                              const float* upper, int32_t split_depth, int64_t node_terminate_thresh, float offset,
+                              int32_t flags, int64_t node_capacity, int64_t* counts_out,
+                              void* workspace, size_t workspace_bytes, void* stream);
+/* Which engine the level-set tree entry points use for a model and options:
+ * NIQ_TREE_ENGINE_TENSOR -- hidden layers' products on the tensor cores (3xTF32, affine_fixed
+ *   with outward rounding, products AUTO or 3XTF32, hidden widths <= 64, a scalar output);
+ * NIQ_TREE_ENGINE_FP32 -- the FP32 tile engine (the other fixed-mode cases);
+ * NIQ_TREE_ENGINE_GROWING -- the growing-term modes, through niq_levelset_tree_growing.
+ * Pure host code; the reference has one engine (XLA), so no counterpart. */
+#define NIQ_TREE_ENGINE_FP32     0
+#define NIQ_TREE_ENGINE_TENSOR   1
+#define NIQ_TREE_ENGINE_GROWING  2
+int niq_tree_engine(const niq_model* model, const niq_bound_opts* opts, int32_t* engine_out);
 /* Device pointers into a finished tree workspace: kind 0 unknown, 1 interior,
  * 2 exterior; lower/upper are (node_capacity, 3) arrays whose first count rows hold
  * the result. */
@@ -329,9 +360,15 @@ int niq_find_any_intersection(const niq_model* model_a, const niq_model* model_b
 
 /* ---- closest point: closest_point (src/kd_tree.py:659-802) -------------------------- *
  * The reference schedule: one global LIFO stack, batch pops of batch_process_size
- * nodes, scatter-min of candidate distances.  Host loop with one sync per batch. */
+ * nodes, scatter-min of candidate distances.  Host loop with one sync per batch.
+ * Every mode: in the growing-term ones (affine_truncate, affine_append, affine_all)
+ * each popped batch is classified by the growing-term engine first, and the workspace
+ * must have niq_closest_point_growing_workspace_size() bytes. */
 size_t niq_closest_point_workspace_size(int64_t n_queries, int32_t batch_process_size,
                                         int64_t stack_capacity);
+size_t niq_closest_point_growing_workspace_size(const niq_model* model, const niq_bound_opts* opts,
+                                                int64_t n_queries, int32_t batch_process_size,
+                                                int64_t stack_capacity);
 int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const float* lower,
                       const float* upper, int64_t n_queries, const float* query_points,
                       float eps, int32_t batch_process_size, int64_t stack_capacity,

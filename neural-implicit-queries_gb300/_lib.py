@@ -95,6 +95,10 @@ _SIGS = {
     'niq_levelset_tree_batches': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _I64,
                                             _P, _P, _SZ, _P]),
     'niq_tree_result': (C.c_int, [_P, _I64, _I32, _I32, C.POINTER(_P), C.POINTER(_P)]),
+    'niq_tree_engine': (C.c_int, [_P, C.POINTER(BoundOpts), C.POINTER(_I32)]),
+    'niq_tree_growing_workspace_size': (_SZ, [_P, C.POINTER(BoundOpts), _I64, _I32]),
+    'niq_levelset_tree_growing': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
+                                            _SZ, _P]),
     'niq_levelset_tree_static': (C.c_int, [_P, _P, _SZ, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32,
                                            _P, _P, _P, _P, _P, _P, _P, _P]),
     'niq_hmc_workspace_size': (_SZ, []),
@@ -106,6 +110,7 @@ _SIGS = {
     'niq_find_any_intersection': (C.c_int, [_P, _P, C.POINTER(BoundOpts), _PF, _PF, _F32, _I64, _P, _P, _P, _P, _SZ,
                                             _P]),
     'niq_closest_point_workspace_size': (_SZ, [_I64, _I32, _I64]),
+    'niq_closest_point_growing_workspace_size': (_SZ, [_P, C.POINTER(BoundOpts), _I64, _I32, _I64]),
     'niq_closest_point': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I64, _P, _F32, _I32, _I64, _P, _P, _P, _SZ,
                                     _P]),
     'niq_closest_point_persistent_workspace_size': (_SZ, [_I64]),

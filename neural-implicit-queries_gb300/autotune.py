@@ -19,7 +19,9 @@ import numpy as np
 
 from . import _io, _lib
 
-PARAMS = {'batched_chunk': 0, 'batched_ctas_per_sm': 1, 'tree_ctas_per_sm': 2}
+PARAMS = {'batched_chunk': 0, 'batched_ctas_per_sm': 1, 'tree_ctas_per_sm': 2,
+          # 1 + the polls a bounded device wait may make (0: built-in limit, 1: give up at once)
+          'barrier_polls': 3, 'mbar_polls': 4}
 CACHE = os.environ.get('NIQ_AUTOTUNE_CACHE', os.path.join(os.path.dirname(__file__), 'niq.autotune.json'))
 
 

@@ -97,13 +97,15 @@ struct CpArgs {
     float prune_tol;         // persistent form: prune when box distance >= best - prune_tol
 };
 
-// ---- reference schedule: process one popped batch [pop, top) of the global stack
-template <int TPI, bool C, bool SLOPE>
+// ---- reference schedule: process one popped batch [pop, top) of the global stack.
+// EXT: the batch's box signs come from ext_type (the growing-term engine classified them
+// beforehand); otherwise the tile engine bounds each box here.
+template <int TPI, bool C, bool SLOPE, bool EXT>
 __global__ void __launch_bounds__(kNT) k_cp_batch(NiqModelRef M, CpArgs a, const float* __restrict__ st_lo,
                                                   const float* __restrict__ st_hi, const int* __restrict__ st_id,
                                                   long long pop, long long n, float* tmp_lo, float* tmp_hi, int* tmp_id,
                                                   float* tmp_d, int* tmp_need, int fixed_floats, int sw_cap,
-                                                  int resident) {
+                                                  int resident, const int* __restrict__ ext_type) {
     using CB = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT>, TileCfg<5, 1, TPI, kNT>>::type;
     using CP = TileCfg<8, 0, TPI, kNT>;
     constexpr int ITEMS = CP::ITEMS;
@@ -130,17 +132,20 @@ __global__ void __launch_bounds__(kNT) k_cp_batch(NiqModelRef M, CpArgs a, const
             s_hi[item][g] = st_hi[3 * (pop + e) + g];
         }
         __syncthreads();
-        box_rows<CB::R, CB::LD, C, SLOPE>(st + item * CB::R * CB::LD, g, valid, s_lo[item], s_hi[item], a.interval, gam0);
-        __syncthreads();
-        tile_forward<CB, C>(H, M.w, sW, sw_cap, resident, pb, st, ob);
-        if (g == 0 && valid) {
-            float lo, hi;
-            if (SLOPE) slope_out_bounds<C>(ob + item * CB::R, pb.v, lo, hi);
-            else affine_out_bounds<CB::R, C>(ob + item * CB::R, pb.v, lo, hi);
-            s_lohi[item][0] = lo;
-            s_lohi[item][1] = hi;
+        if (!EXT) {
+            box_rows<CB::R, CB::LD, C, SLOPE>(st + item * CB::R * CB::LD, g, valid, s_lo[item], s_hi[item], a.interval,
+                                              gam0);
+            __syncthreads();
+            tile_forward<CB, C>(H, M.w, sW, sw_cap, resident, pb, st, ob);
+            if (g == 0 && valid) {
+                float lo, hi;
+                if (SLOPE) slope_out_bounds<C>(ob + item * CB::R, pb.v, lo, hi);
+                else affine_out_bounds<CB::R, C>(ob + item * CB::R, pb.v, lo, hi);
+                s_lohi[item][0] = lo;
+                s_lohi[item][1] = hi;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         {
             float c[3], s[3];
             for (int k = 0; k < 3; ++k) {
@@ -155,7 +160,7 @@ __global__ void __launch_bounds__(kNT) k_cp_batch(NiqModelRef M, CpArgs a, const
             const float* lo = s_lo[item];
             const float* hi = s_hi[item];
             const int id = st_id[pop + e];
-            const int type = sign_of_bounds(s_lohi[item][0], s_lohi[item][1], 0.f);
+            const int type = EXT ? ext_type[e] : sign_of_bounds(s_lohi[item][0], s_lohi[item][1], 0.f);
             const bool outside = type != NIQ_SIGN_UNKNOWN;
             float c[3], w[3];
             for (int k = 0; k < 3; ++k) { c[k] = __fmul_rn(0.5f, __fadd_rn(lo[k], hi[k])); w[k] = __fsub_rn(hi[k], lo[k]); }
@@ -413,7 +418,7 @@ template <int TPI, bool C, bool SLOPE>
 __global__ void __launch_bounds__(kNT) k_intersect(NiqModelRef MA, NiqModelRef MB, int interval, float eps_w,
                                                    IsWs* ws, float* lv_lo0, float* lv_hi0, float* lv_lo1, float* lv_hi1,
                                                    long long cap, int woffB, int fixed_floats, int sw_cap,
-                                                   int resident) {
+                                                   int resident, unsigned int polls) {
     using CB = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT>, TileCfg<5, 1, TPI, kNT>>::type;
     using CP = TileCfg<8, 0, TPI, kNT>;
     constexpr int ITEMS = CP::ITEMS;
@@ -551,7 +556,7 @@ __global__ void __launch_bounds__(kNT) k_intersect(NiqModelRef MA, NiqModelRef M
                 }
             }
         }
-        if (!niq_grid_barrier(&ws->barrier, gridDim.x, epoch, &ws->err)) break;
+        if (!niq_grid_barrier(&ws->barrier, gridDim.x, epoch, &ws->err, polls)) break;
     }
     __syncthreads();
     if (threadIdx.x == 0 && s_proc) atomicAdd(&ws->processed, s_proc);
@@ -692,6 +697,39 @@ int cp_plan(K kern, const niq_model* m, int R, int TPIv, SmemPlan& p) {
     return prepare_kernel(kern, p.bytes);
 }
 
+// Boxes [pop, pop + n) of the stack as center + diagonal vectors (src/implicit_function.py:33-37)
+// for the growing-term engine.
+__global__ void k_cp_boxes(const float* st_lo, const float* st_hi, long long pop, long long n, int cons, float* center,
+                           float* vecs) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 3; ++k) {
+        const float l = st_lo[3 * (pop + i) + k], h = st_hi[3 * (pop + i) + k];
+        const float c = __fmul_rn(0.5f, __fadd_rn(l, h));
+        const float half = cons ? fmaxf(__fsub_ru(h, c), __fsub_ru(c, l)) : __fsub_rn(h, c);
+        center[3 * i + k] = c;
+        for (int j = 0; j < 3; ++j) vecs[9 * i + 3 * k + j] = j == k ? half : 0.f;
+    }
+}
+
+// Scratch of the growing-term modes after the reference schedule's layout.
+struct CpGrowLayout {
+    size_t center, vecs, type, cws, cws_bytes, total;
+};
+
+CpGrowLayout cp_grow_layout(const niq_model* m, const niq_bound_opts* opts, size_t base, long long B) {
+    CpGrowLayout G;
+    size_t off = al256(base);
+    G.center = off; off += al256((size_t)B * 12);
+    G.vecs = off; off += al256((size_t)B * 36);
+    G.type = off; off += al256((size_t)B * 4);
+    G.cws = off;
+    G.cws_bytes = niq_classify_workspace_size(m, opts, B, 3);
+    off += al256(G.cws_bytes);
+    G.total = off + 256;
+    return G;
+}
+
 }  // namespace
 
 extern "C" {
@@ -700,17 +738,26 @@ size_t niq_closest_point_workspace_size(int64_t n_queries, int32_t batch_process
     return cp_layout(n_queries, batch_process_size, stack_capacity).total;
 }
 
+size_t niq_closest_point_growing_workspace_size(const niq_model* model, const niq_bound_opts* opts, int64_t n_queries,
+                                                int32_t batch_process_size, int64_t stack_capacity) {
+    if (!model || !opts || batch_process_size < 1) return 0;
+    return cp_grow_layout(model, opts, cp_layout(n_queries, batch_process_size, stack_capacity).total,
+                          batch_process_size).total;
+}
+
 int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const float* lower, const float* upper,
                       int64_t n_queries, const float* query_points, float eps, int32_t batch_process_size,
                       int64_t stack_capacity, float* min_dist_out, float* min_loc_out, void* workspace,
                       size_t workspace_bytes, void* stream) {
     NIQ_REQUIRE(model && opts && lower && upper, NIQ_ERR_INVALID_ARG, "null argument");
-    NIQ_REQUIRE(fixed_mode(opts->mode), NIQ_ERR_UNSUPPORTED, "closest_point supports interval, affine_fixed, slope_interval");
     NIQ_REQUIRE(n_queries >= 0 && n_queries < (1ll << 31) && batch_process_size >= 1, NIQ_ERR_INVALID_ARG, "bad sizes");
     NIQ_REQUIRE(stack_capacity >= n_queries + 2 * (long long)batch_process_size, NIQ_ERR_INVALID_ARG,
                 "stack_capacity must be >= n_queries + 2 * batch_process_size");
     const CpLayout CL = cp_layout(n_queries, batch_process_size, stack_capacity);
-    NIQ_REQUIRE(workspace && workspace_bytes >= CL.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", CL.total);
+    const bool growing = !fixed_mode(opts->mode);
+    const CpGrowLayout GL = cp_grow_layout(model, opts, CL.total, batch_process_size);
+    const size_t need = growing ? GL.total : CL.total;
+    NIQ_REQUIRE(workspace && workspace_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", need);
     if (n_queries == 0) return NIQ_OK;
     NIQ_REQUIRE(query_points && min_dist_out && min_loc_out, NIQ_ERR_INVALID_ARG, "null array");
     cudaStream_t s = as_stream(stream);
@@ -746,6 +793,10 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
     const bool cons = opts->conservative != 0, slope = opts->mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(model->hdr.max_width);
     int rc = NIQ_OK;
+    float* g_center = reinterpret_cast<float*>(b + GL.center);
+    float* g_vecs = reinterpret_cast<float*>(b + GL.vecs);
+    int* g_type = reinterpret_cast<int*>(b + GL.type);
+    void* g_cws = b + GL.cws;
     auto run = [&](auto kern, int TPIv) -> int {
         SmemPlan p;
         int r2 = cp_plan(kern, model, 8, TPIv, p);
@@ -760,9 +811,18 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
             const long long pop = top - B > 0 ? top - B : 0;
             const long long n = top - pop;
             const long long tiles = (n + items - 1) / items;
+            if (growing) {
+                // the batch's boxes through the growing-term engine first
+                k_cp_boxes<<<(int)((n + 255) / 256), 256, 0, s>>>(st_lo, st_hi, pop, n, opts->conservative != 0,
+                                                                  g_center, g_vecs);
+                NIQ_CUDA(cudaGetLastError());
+                const int rc2 = niq_classify_boxes(model, opts, n, g_center, g_vecs, 3, 0.f, g_type, nullptr, g_cws,
+                                                   GL.cws_bytes, stream);
+                if (rc2) return rc2;
+            }
             kern<<<(int)(tiles < grid_max ? tiles : grid_max), kNT, p.bytes, s>>>(
                 model->ref(), a, st_lo, st_hi, st_id, pop, n, t_lo, t_hi, t_id, t_d, t_need, p.fixed_floats, p.sw_cap,
-                p.resident);
+                p.resident, g_type);
             NIQ_CUDA(cudaGetLastError());
             k_cp_finish<<<1, 1024, 0, s>>>(a, pop, n, t_lo, t_hi, t_id, t_d, t_need, st_lo, st_hi, st_id,
                                            stack_capacity, top_d, err);
@@ -776,8 +836,9 @@ int niq_closest_point(const niq_model* model, const niq_bound_opts* opts, const 
         }
         return NIQ_OK;
     };
-#define NIQ_CP(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_cp_batch<TPI, CC, SL>, TPI); })
-    if (slope) { if (cons) { NIQ_CP(true, true); } else { NIQ_CP(false, true); } }
+#define NIQ_CP(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_cp_batch<TPI, CC, SL, false>, TPI); })
+    if (growing) { NIQ_DISPATCH_TPI(tpi, { rc = run(k_cp_batch<TPI, false, false, true>, TPI); }); }
+    else if (slope) { if (cons) { NIQ_CP(true, true); } else { NIQ_CP(false, true); } }
     else { if (cons) { NIQ_CP(true, false); } else { NIQ_CP(false, false); } }
 #undef NIQ_CP
     return rc;
@@ -904,7 +965,9 @@ int niq_find_any_intersection(const niq_model* model_a, const niq_model* model_b
             long long cap = node_capacity;
             int woffB = model_a->hdr.n_weight_floats;
             int fixed = p.fixed_floats, swc = p.sw_cap, res = p.resident;
-            void* args[] = {&A, &Bm, &interval, &ew, &ws, &lv[0], &lv[1], &lv[2], &lv[3], &cap, &woffB, &fixed, &swc, &res};
+            unsigned int polls = barrier_polls();
+            void* args[] = {&A, &Bm, &interval, &ew, &ws, &lv[0], &lv[1], &lv[2], &lv[3], &cap, &woffB, &fixed, &swc, &res,
+                            &polls};
             NIQ_CUDA(cudaLaunchCooperativeKernel((const void*)kern, grid, kNT, args, p.bytes, s));
             return NIQ_OK;
         };

@@ -14,43 +14,9 @@
 // size after each (the plain form, as the reference's per-level host loop).
 // Node order inside a level is whatever the atomics produce; results are node sets.
 #include <mutex>
-#include "niq_host.cuh"
+#include "tree_common.cuh"
 
 namespace niq {
-
-constexpr int kTreeMaxLevels = 64;
-
-struct TreeWs {
-    unsigned long long level_count[kTreeMaxLevels + 1];  // nodes of level L (append counter)
-    unsigned long long grab[kTreeMaxLevels + 1];         // claim counter of level L
-    unsigned long long n_unknown, n_interior, n_exterior, n_boxes;
-    unsigned int barrier;
-    int err;
-    int last_level;
-    int pad;
-};
-
-struct TreeBufs {
-    float* lvl_lo[2];
-    float* lvl_hi[2];
-    float* res_lo[3];   // unknown, interior, exterior
-    float* res_hi[3];
-    long long cap;
-};
-
-struct TreeParams {
-    int n_rounds;               // split_depth + 1, or kTreeMaxLevels
-    long long thresh;           // node_terminate_thresh (huge when unset)
-    float offset;
-    int with_interior, with_exterior;
-    int mode_interval;
-    long long batch_start, batch_end;   // node range of the level this launch covers
-};
-
-__device__ __forceinline__ void put_node(float* lo, float* hi, long long i, const float* a, const float* b) {
-    lo[3 * i] = a[0]; lo[3 * i + 1] = a[1]; lo[3 * i + 2] = a[2];
-    hi[3 * i] = b[0]; hi[3 * i + 1] = b[1]; hi[3 * i + 2] = b[2];
-}
 
 template <int TPI, bool C, bool SLOPE, bool COOP>
 __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeWs* ws, TreeBufs B, int level0,
@@ -203,7 +169,7 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
             if (blockIdx.x == 0 && threadIdx.x == 0) ws->last_level = L;
             break;
         }
-        if (!niq_grid_barrier(&ws->barrier, gridDim.x, epoch, &ws->err)) break;
+        if (!niq_grid_barrier(&ws->barrier, gridDim.x, epoch, &ws->err, P.barrier_polls)) break;
     }
     __syncthreads();
     if (threadIdx.x == 0 && s_boxes) atomicAdd(&ws->n_boxes, s_boxes);
@@ -249,6 +215,25 @@ __global__ void k_tree_finish(TreeWs* ws, long long* counts) {
     counts[3] = (long long)ws->n_boxes;
 }
 
+// The tensor-core tree serves affine_fixed with outward rounding unless FP32 products
+// are asked for, on the models it supports.
+static bool use_tree_tc(const NiqSpecHeader& H, const niq_bound_opts* opts) {
+    return opts->mode == NIQ_MODE_AFFINE_FIXED && opts->conservative != 0 && opts->products != NIQ_PRODUCTS_FP32 &&
+           tree_tc_eligible(H);
+}
+
+// Counts to the caller's array, then the kernels' error status (syncs the stream).
+static int finish_tree(TreeWs* ws, long long* counts, long long cap, cudaStream_t s) {
+    k_tree_finish<<<1, 1, 0, s>>>(ws, counts);
+    NIQ_CUDA(cudaGetLastError());
+    int err = 0;
+    NIQ_CUDA(cudaMemcpyAsync(&err, &ws->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    NIQ_REQUIRE(err == 0, err, err == NIQ_ERR_CAPACITY ? "node capacity %lld exceeded" : "tree kernel error (%lld)",
+                err == NIQ_ERR_CAPACITY ? cap : (long long)err);
+    return NIQ_OK;
+}
+
 template <bool COOP>
 static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float* lower, const float* upper,
                     int split_depth, long long thresh, float offset, int flags, long long cap, long long* counts,
@@ -281,9 +266,17 @@ static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float*
     P.mode_interval = mode == NIQ_MODE_INTERVAL;
     P.batch_start = 0;
     P.batch_end = 1ll << 62;
+    P.barrier_polls = barrier_polls();
+    P.mbar_polls = mbar_polls();
     const bool cons = opts->conservative != 0, slope = mode == NIQ_MODE_SLOPE_INTERVAL;
     const int tpi = tpi_for_width(m->hdr.max_width);
     int rc = NIQ_OK;
+    if (use_tree_tc(m->hdr, opts)) {
+        TreeLaunch T{m->ref(), &m->hdr, P, ws, B, s, COOP, batch};
+        rc = run_tree_tc(T);
+        if (rc) return rc;
+        return finish_tree(ws, counts, cap, s);
+    }
     auto run = [&](auto kern, int R, int TPIv) -> int {
         const int items = kNT / TPIv;
         const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
@@ -335,14 +328,7 @@ static int run_tree(const niq_model* m, const niq_bound_opts* opts, const float*
     else { if (cons) { NIQ_TREE(true, false); } else { NIQ_TREE(false, false); } }
 #undef NIQ_TREE
     if (rc) return rc;
-    k_tree_finish<<<1, 1, 0, s>>>(ws, counts);
-    NIQ_CUDA(cudaGetLastError());
-    int err = 0;
-    NIQ_CUDA(cudaMemcpyAsync(&err, &ws->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    NIQ_CUDA(cudaStreamSynchronize(s));
-    NIQ_REQUIRE(err == 0, err, err == NIQ_ERR_CAPACITY ? "node capacity %lld exceeded" : "tree kernel error (%lld)",
-                err == NIQ_ERR_CAPACITY ? cap : (long long)err);
-    return NIQ_OK;
+    return finish_tree(ws, counts, cap, s);
 }
 
 }  // namespace niq
@@ -379,6 +365,16 @@ int niq_levelset_tree_batches(const niq_model* model, const niq_bound_opts* opts
                            batch_process_size);
 }
 
+int niq_tree_engine(const niq_model* model, const niq_bound_opts* opts, int32_t* engine_out) {
+    NIQ_REQUIRE(model && opts && engine_out, NIQ_ERR_INVALID_ARG, "null argument");
+    const int mode = opts->mode;
+    if (mode == NIQ_MODE_AFFINE_TRUNCATE || mode == NIQ_MODE_AFFINE_APPEND || mode == NIQ_MODE_AFFINE_ALL)
+        *engine_out = NIQ_TREE_ENGINE_GROWING;
+    else
+        *engine_out = use_tree_tc(model->hdr, opts) ? NIQ_TREE_ENGINE_TENSOR : NIQ_TREE_ENGINE_FP32;
+    return NIQ_OK;
+}
+
 int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32_t kind, float** lower, float** upper) {
     NIQ_REQUIRE(workspace && lower && upper && kind >= 0 && kind <= 2, NIQ_ERR_INVALID_ARG, "bad argument");
     NIQ_REQUIRE(kind != 1 || (flags & NIQ_TREE_WITH_INTERIOR), NIQ_ERR_INVALID_ARG, "tree built without interior nodes");
@@ -391,6 +387,167 @@ int niq_tree_result(void* workspace, int64_t node_capacity, int32_t flags, int32
 }
 
 }  // extern "C"
+
+// ==========================================================================================
+// Growing-term modes (affine_truncate, affine_append, affine_all): the reference's level
+// loop (src/kd_tree.py:137-198) over the growing-term engine of niq_classify_boxes.  Each
+// level is cut into chunks of kTreeGrowChunk nodes: a kernel writes their boxes as
+// center + diagonal vectors (src/implicit_function.py:33-37), the engine classifies them,
+// and a second kernel appends results and children exactly as k_tree does; the host reads
+// the next level's size.  Any mode is accepted (the fixed ones give k_tree's node sets).
+// ==========================================================================================
+namespace niq {
+
+constexpr long long kTreeGrowChunk = 1 << 16;
+
+__global__ void k_tree_boxes(const float* lo, const float* hi, long long s, long long n, int cons, float* center,
+                             float* vecs) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float l = lo[3 * (s + i) + k], h = hi[3 * (s + i) + k];
+        const float c = __fmul_rn(0.5f, __fadd_rn(l, h));
+        const float half = cons ? fmaxf(__fsub_ru(h, c), __fsub_ru(c, l)) : __fsub_rn(h, c);
+        center[3 * i + k] = c;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) vecs[9 * i + 3 * k + j] = j == k ? half : 0.f;
+    }
+}
+
+// Results and children of nodes s .. s + n - 1 of level L from their signs (k_tree's
+// consume step, one thread per node; every lane of a warp joins the votes).
+__global__ void k_tree_consume(const int* sign, long long s, long long n, int quit, TreeParams P, TreeWs* ws, TreeBufs B,
+                               int L) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const long long nid = s + i;
+    const int type = valid ? sign[i] : -1;
+    const bool is_unknown = type == NIQ_SIGN_UNKNOWN;
+    const bool is_int = P.with_interior && type == NIQ_SIGN_NEGATIVE;
+    const bool is_ext = P.with_exterior && type == NIQ_SIGN_POSITIVE;
+    const long long pi = niq_warp_reserve(&ws->n_interior, is_int, 1);
+    const long long pe = niq_warp_reserve(&ws->n_exterior, is_ext, 1);
+    const long long pu = quit ? niq_warp_reserve(&ws->n_unknown, is_unknown, 1) : -1;
+    const long long pc = quit ? -1 : niq_warp_reserve(&ws->level_count[L + 1], is_unknown, 2);
+    niq_warp_reserve(&ws->n_boxes, valid, 1);
+    if (!valid) return;
+    const float* in_lo = B.lvl_lo[L & 1];
+    const float* in_hi = B.lvl_hi[L & 1];
+    const float lo[3] = {in_lo[3 * nid], in_lo[3 * nid + 1], in_lo[3 * nid + 2]};
+    const float hi[3] = {in_hi[3 * nid], in_hi[3 * nid + 1], in_hi[3 * nid + 2]};
+    if (is_int) { if (pi < B.cap) put_node(B.res_lo[1], B.res_hi[1], pi, lo, hi); else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY); }
+    if (is_ext) { if (pe < B.cap) put_node(B.res_lo[2], B.res_hi[2], pe, lo, hi); else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY); }
+    if (!is_unknown) return;
+    if (quit) {
+        if (pu < B.cap) put_node(B.res_lo[0], B.res_hi[0], pu, lo, hi);
+        else niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+        return;
+    }
+    if (pc + 1 >= B.cap) {
+        niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+        return;
+    }
+    // split along the first longest axis (src/kd_tree.py:38,70-77)
+    const float e0 = __fsub_rn(hi[0], lo[0]), e1 = __fsub_rn(hi[1], lo[1]), e2 = __fsub_rn(hi[2], lo[2]);
+    int d = 0;
+    float em = e0;
+    if (e1 > em) { d = 1; em = e1; }
+    if (e2 > em) { d = 2; }
+    const float mid = d == 0 ? __fmul_rn(0.5f, __fadd_rn(lo[0], hi[0]))
+                    : d == 1 ? __fmul_rn(0.5f, __fadd_rn(lo[1], hi[1]))
+                             : __fmul_rn(0.5f, __fadd_rn(lo[2], hi[2]));
+    const float ahi[3] = {d == 0 ? mid : hi[0], d == 1 ? mid : hi[1], d == 2 ? mid : hi[2]};
+    const float blo[3] = {d == 0 ? mid : lo[0], d == 1 ? mid : lo[1], d == 2 ? mid : lo[2]};
+    float* out_lo = B.lvl_lo[(L + 1) & 1];
+    float* out_hi = B.lvl_hi[(L + 1) & 1];
+    put_node(out_lo, out_hi, pc, lo, ahi);
+    put_node(out_lo, out_hi, pc + 1, blo, hi);
+}
+
+// Scratch after the tree layout: chunk boxes (center, vecs), signs, the engine's workspace.
+struct GrowLayout {
+    size_t center, vecs, sign, cws, cws_bytes, total;
+};
+
+static GrowLayout grow_layout(const niq_model* m, const niq_bound_opts* opts, long long cap, int flags) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    GrowLayout G;
+    size_t off = al(tree_layout(cap, flags).total);
+    G.center = off; off += al((size_t)kTreeGrowChunk * 12);
+    G.vecs = off; off += al((size_t)kTreeGrowChunk * 36);
+    G.sign = off; off += al((size_t)kTreeGrowChunk * 4);
+    G.cws = off;
+    G.cws_bytes = niq_classify_workspace_size(m, opts, kTreeGrowChunk, 3);
+    off += al(G.cws_bytes);
+    G.total = off + 256;
+    return G;
+}
+
+}  // namespace niq
+
+extern "C" size_t niq_tree_growing_workspace_size(const niq_model* model, const niq_bound_opts* opts,
+                                                  int64_t node_capacity, int32_t flags) {
+    if (!model || !opts || node_capacity < 2) return 0;
+    return niq::grow_layout(model, opts, node_capacity, flags).total;
+}
+
+extern "C" int niq_levelset_tree_growing(const niq_model* model, const niq_bound_opts* opts, const float* lower,
+                                         const float* upper, int32_t split_depth, int64_t node_terminate_thresh,
+                                         float offset, int32_t flags, int64_t node_capacity, int64_t* counts_out,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+    using namespace niq;
+    NIQ_REQUIRE(model && opts && lower && upper && counts_out, NIQ_ERR_INVALID_ARG, "null argument");
+    NIQ_REQUIRE(split_depth >= 0 || node_terminate_thresh > 0, NIQ_ERR_INVALID_ARG,
+                "must specify at least one of node_terminate_thresh or split_depth as a terminating condition");
+    NIQ_REQUIRE(split_depth < kTreeMaxLevels, NIQ_ERR_INVALID_ARG, "split_depth %d exceeds %d", split_depth,
+                kTreeMaxLevels - 1);
+    NIQ_REQUIRE(node_capacity >= 2, NIQ_ERR_INVALID_ARG, "node capacity too small");
+    const GrowLayout G = grow_layout(model, opts, node_capacity, flags);
+    NIQ_REQUIRE(workspace && workspace_bytes >= G.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", G.total);
+    cudaStream_t s = as_stream(stream);
+    TreeBufs B;
+    tree_bufs(workspace, node_capacity, flags, B);
+    char* base = ws_base(workspace);
+    TreeWs* ws = reinterpret_cast<TreeWs*>(base);
+    float* center = reinterpret_cast<float*>(base + G.center);
+    float* vecs = reinterpret_cast<float*>(base + G.vecs);
+    int* sign = reinterpret_cast<int*>(base + G.sign);
+    void* cws = base + G.cws;
+    NIQ_CUDA(cudaMemsetAsync(ws, 0, sizeof(TreeWs), s));
+    NIQ_CUDA(cudaMemcpyAsync(B.lvl_lo[0], lower, 12, cudaMemcpyHostToDevice, s));
+    NIQ_CUDA(cudaMemcpyAsync(B.lvl_hi[0], upper, 12, cudaMemcpyHostToDevice, s));
+    const unsigned long long one = 1;
+    NIQ_CUDA(cudaMemcpyAsync(&ws->level_count[0], &one, 8, cudaMemcpyHostToDevice, s));
+    TreeParams P{};
+    P.n_rounds = split_depth >= 0 ? split_depth + 1 : kTreeMaxLevels;
+    P.thresh = node_terminate_thresh > 0 ? node_terminate_thresh : (1ll << 62);
+    P.offset = offset;
+    P.with_interior = (flags & NIQ_TREE_WITH_INTERIOR) != 0;
+    P.with_exterior = (flags & NIQ_TREE_WITH_EXTERIOR) != 0;
+    const int cons = opts->conservative != 0;
+    for (int L = 0; L < kTreeMaxLevels; ++L) {
+        unsigned long long cnt = 0;
+        NIQ_CUDA(cudaMemcpyAsync(&cnt, &ws->level_count[L], 8, cudaMemcpyDeviceToHost, s));
+        NIQ_CUDA(cudaStreamSynchronize(s));
+        const long long n_in = (long long)cnt;
+        if (n_in > node_capacity) break;   // reported by the capacity flag of the level before
+        const bool quit = (n_in >= P.thresh) || (L + 1 >= P.n_rounds) || (n_in == 0) || (L + 1 == kTreeMaxLevels);
+        for (long long c0 = 0; c0 < n_in; c0 += kTreeGrowChunk) {
+            const long long n = n_in - c0 < kTreeGrowChunk ? n_in - c0 : kTreeGrowChunk;
+            const int blocks = (int)((n + 255) / 256);
+            k_tree_boxes<<<blocks, 256, 0, s>>>(B.lvl_lo[L & 1], B.lvl_hi[L & 1], c0, n, cons, center, vecs);
+            NIQ_CUDA(cudaGetLastError());
+            const int rc = niq_classify_boxes(model, opts, n, center, vecs, 3, offset, sign, nullptr, cws, G.cws_bytes,
+                                              stream);
+            if (rc) return rc;
+            k_tree_consume<<<blocks, 256, 0, s>>>(sign, c0, n, quit ? 1 : 0, P, ws, B, L);
+            NIQ_CUDA(cudaGetLastError());
+        }
+        if (quit) break;
+    }
+    return finish_tree(ws, reinterpret_cast<long long*>(counts_out), node_capacity, s);
+}
 
 // ==========================================================================================
 // Level-set tree without device allocation.
@@ -514,6 +671,8 @@ extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void
     P.mode_interval = mode == NIQ_MODE_INTERVAL;
     P.batch_start = 0;
     P.batch_end = 1ll << 62;
+    P.barrier_polls = barrier_polls();
+    P.mbar_polls = mbar_polls();
     NiqModelRef M;
     M.hdr = reinterpret_cast<const NiqSpecHeader*>(packed_spec_device);
     M.w = reinterpret_cast<const float*>(reinterpret_cast<const char*>(packed_spec_device) + sizeof(NiqSpecHeader));
@@ -539,7 +698,11 @@ extern "C" int niq_levelset_tree_static(const void* packed_spec_host, const void
         return NIQ_OK;
     };
 #define NIQ_TREE_S(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_tree<TPI, CC, SL, true>, SL ? 8 : 5, TPI); })
-    if (slope) { if (cons) { NIQ_TREE_S(true, true); } else { NIQ_TREE_S(false, true); } }
+    if (use_tree_tc(H, opts)) {
+        // the same kernel as niq_levelset_tree picks for this model (no allocation either)
+        TreeLaunch T{M, &H, P, ws, B, s, true, 0};
+        rc = run_tree_tc(T);
+    } else if (slope) { if (cons) { NIQ_TREE_S(true, true); } else { NIQ_TREE_S(false, true); } }
     else { if (cons) { NIQ_TREE_S(true, false); } else { NIQ_TREE_S(false, false); } }
 #undef NIQ_TREE_S
     if (rc) return rc;

@@ -42,7 +42,6 @@ constexpr int kTcTrLD = 17;                    // transpose buffer row stride (1
 constexpr int kTcStages = 3;                   // shared-memory pipeline depth
 constexpr int kTcStage = 4 * kTcRows * kTcKC;  // floats: X hi, X lo, W hi, W lo
 constexpr int kTcXFloats = kTcRows * NIQ_MAX_WIDTH;  // one split half of a CTA's X scratch
-constexpr long long kTcPolls = 1ll << 24;      // mbarrier polls before a wait gives up
 
 // dynamic shared memory (floats)
 constexpr int kTcOffTr = kTcStages * kTcStage;
@@ -67,6 +66,7 @@ struct TcArgs {
     float* lohi_out;
     float* xs;                         // per CTA: 2 * kTcXFloats (hi, lo)
     int* status;
+    long long mbar_polls;              // poll limit of the waits on the MMAs
 };
 
 NIQ_HOST_DEVICE int round16(int x) { return (x + 15) & ~15; }
@@ -180,11 +180,15 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     const int K = mode == NIQ_MODE_AFFINE_TRUNCATE ? a.opts.truncate_count : kTcRows;
     bool fail = false;
 
-    auto wait_stage = [&](int s) -> bool {
+    // A wait that gives up leaves the stage pending, so the unwind below waits for it again
+    // (with the built-in limit) before the tensor memory is released.
+    auto wait_stage = [&](int s, long long limit) -> bool {
         if (!((pending >> s) & 1u)) return true;
-        const bool ok = tc::mbar_wait(&bar[s], (phase >> s) & 1u, kTcPolls);
-        phase ^= 1u << s;
-        pending &= ~(1u << s);
+        const bool ok = tc::mbar_wait(&bar[s], (phase >> s) & 1u, limit);
+        if (ok) {
+            phase ^= 1u << s;
+            pending &= ~(1u << s);
+        }
         return ok;
     };
 
@@ -266,7 +270,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 auto load_chunk = [&](int c) {
                     if (c < chunks) {
                         const int s = c % kTcStages;
-                        if (!wait_stage(s)) fail = true;   // the MMAs that last read this stage
+                        if (!wait_stage(s, a.mbar_polls)) fail = true;   // the MMAs that last read this stage
+                    }
+                    if (c < chunks && !fail) {   // no copy into a stage whose MMAs may still read it
+                        const int s = c % kTcStages;
                         float* stg = smem + s * kTcStage;
                         const int xf4 = mt * 128 * kTcKC / 4, wf4 = o16 * kTcKC / 4;
                         const float* xsrc_h = xs_hi + c * kTcRows * kTcKC;
@@ -291,7 +298,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     float* stg = smem + s * kTcStage;
                     cp_async_wait_but_one();   // chunk c has landed (chunk c + 1 may be in flight)
                     tc::fence_async_smem();
-                    __syncthreads();           // also: every thread is done with iteration c - 1
+                    // also: every thread is done with iteration c - 1, and all agree on `fail`
+                    fail = __syncthreads_or(fail ? 1 : 0) != 0;
                     if (tid == 0 && !fail) {
                         tc::fence_after_sync();
                         const uint32_t xh = tc::smem_addr(stg), xl = xh + kTcRows * kTcKC * 4;
@@ -313,7 +321,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         }
                         tc::mma_commit(&bar[s]);
                     }
-                    pending |= 1u << s;
+                    if (!fail) pending |= 1u << s;
                     // the stage of chunk c + 2 held chunk c - 1: every thread finished with it
                     // (the barrier above); its MMAs are waited for inside load_chunk
                     load_chunk(c + 2);
@@ -342,7 +350,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 // every MMA of the layer complete before TMEM is read; a wait that gave up
                 // anywhere in the CTA ends the kernel for every thread
                 for (int s = 0; s < kTcStages; ++s)
-                    if (!wait_stage(s)) fail = true;
+                    if (!wait_stage(s, a.mbar_polls)) fail = true;
                 tc::fence_after_sync();
                 fail = __syncthreads_or(fail ? 1 : 0) != 0;   // also: every thread read the old vectors
                 if (fail) {
@@ -544,7 +552,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     }
     // unwind: wait (bounded) for MMAs still in flight, then free TMEM
     for (int s = 0; s < kTcStages; ++s)
-        if (!wait_stage(s) && tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
+        if (!wait_stage(s, kMbarPollsDefault) && tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -647,6 +655,7 @@ int wide_tc_classify(const niq_model* m, const niq_bound_opts& o, long long n, c
     a.lohi_out = lohi_out;
     char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
     a.status = reinterpret_cast<int*>(base);
+    a.mbar_polls = mbar_polls();
     a.xs = reinterpret_cast<float*>(base + 256);
     NIQ_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), s));
     long long grid = device_info().sm_count;

@@ -83,10 +83,11 @@ __device__ __forceinline__ void niq_flag_error(int* flag, int code) {
 
 // Grid-wide barrier for cooperative launches (all CTAs co-resident).  `ctr` counts
 // arrivals monotonically; `epoch` is the number of barriers this CTA has passed.  The
-// spin is bounded: after ~2^28 polls (seconds) it records NIQ_ERR_TIMEOUT in `err` and
-// returns false so the caller can unwind instead of hanging.
+// spin is bounded: after max_polls polls (2^28 by default, seconds) it records
+// NIQ_ERR_TIMEOUT in `err` and returns false so the caller can unwind instead of
+// hanging; max_polls = 0 gives up without polling.
 __device__ __forceinline__ bool niq_grid_barrier(unsigned int* ctr, unsigned int nblocks,
-                                                 unsigned int& epoch, int* err) {
+                                                 unsigned int& epoch, int* err, unsigned int max_polls) {
     __syncthreads();
     bool ok = true;
     if (threadIdx.x == 0) {
@@ -96,9 +97,9 @@ __device__ __forceinline__ bool niq_grid_barrier(unsigned int* ctr, unsigned int
         atomicAdd(ctr, 1u);
         unsigned int polls = 0;
         while (true) {
+            if (polls++ >= max_polls) { niq_flag_error(err, NIQ_ERR_TIMEOUT); ok = false; break; }
             unsigned int v = *((volatile unsigned int*)ctr);
             if (v >= target) break;
-            if (++polls > (1u << 28)) { niq_flag_error(err, NIQ_ERR_TIMEOUT); ok = false; break; }
             if (err && *((volatile int*)err) != 0) { ok = false; break; }
             __nanosleep(64);
         }

@@ -11,8 +11,23 @@ namespace niq {
 
 void set_error(const char* fmt, ...);
 // Launch parameters an autotuner may set (niq_tune_set); 0 means the built-in choice.
-enum TuneParam : int { kTuneBatchedChunk = 0, kTuneBatchedCtasPerSm = 1, kTuneTreeCtasPerSm = 2, kTuneCount = 3 };
+enum TuneParam : int {
+    kTuneBatchedChunk = 0, kTuneBatchedCtasPerSm = 1, kTuneTreeCtasPerSm = 2, kTuneBarrierPolls = 3,
+    kTuneMbarPolls = 4, kTuneCount = 5
+};
 int tune_value(int param);
+// Poll limits of the bounded device-side waits: the tuned value minus one, or the
+// built-in limits (grid barrier 2^28 polls, mbarrier 2^24) when it is 0.
+constexpr unsigned int kBarrierPollsDefault = 1u << 28;
+constexpr long long kMbarPollsDefault = 1ll << 24;
+inline unsigned int barrier_polls() {
+    const int v = tune_value(kTuneBarrierPolls);
+    return v > 0 ? (unsigned int)(v - 1) : kBarrierPollsDefault;
+}
+inline long long mbar_polls() {
+    const int v = tune_value(kTuneMbarPolls);
+    return v > 0 ? (long long)(v - 1) : kMbarPollsDefault;
+}
 // Checks a packed spec header against its byte size (capi.cu).
 int validate_spec(const NiqSpecHeader& H, size_t bytes);
 int cuda_fail(cudaError_t e, const char* where);

@@ -24,6 +24,9 @@ def _host3(x):
     return (_lib.C.c_float * 3)(*a.tolist())
 
 
+GROWING_MODES = ('affine_truncate', 'affine_append', 'affine_all')
+
+
 def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh, flags, offset, persistent,
                  batch_process_size=2048):
     """Runs the tree on the device; returns (workspace tensor, capacity, counts, model).
@@ -38,7 +41,11 @@ def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh,
         cap = max(64, min(cap, 2 ** (split_depth + 1)))
     key = (m.fingerprint, split_depth, node_terminate_thresh, flags, float(offset), bo.mode, bo.conservative)
     cap = max(cap, _TREE_CAP_SEEN.get(key, 0))
-    if persistent == 'batches':
+    growing = func.mode in GROWING_MODES
+    if growing:
+        # the growing-term modes: the level loop over the growing-term engine (every schedule)
+        fn = L.niq_levelset_tree_growing
+    elif persistent == 'batches':
         B = int(batch_process_size)
 
         def fn(*a):
@@ -46,7 +53,8 @@ def _tree_device(func, params, lower, upper, split_depth, node_terminate_thresh,
     else:
         fn = L.niq_levelset_tree if persistent else L.niq_levelset_tree_plain
     while True:
-        ws_bytes = L.niq_tree_workspace_size(cap, flags)
+        ws_bytes = (L.niq_tree_growing_workspace_size(m.handle, _lib.C.byref(bo), cap, flags) if growing
+                    else L.niq_tree_workspace_size(cap, flags))
         ws = t.empty(ws_bytes, dtype=t.uint8, device='cuda')
         counts = t.zeros(4, dtype=t.int64, device='cuda')
         try:
@@ -218,6 +226,9 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
     dist = t.empty(Q, dtype=t.float32, device='cuda')
     loc = t.empty((Q, 3), dtype=t.float32, device='cuda')
     L = _lib.load()
+    if persistent and func.mode in GROWING_MODES:
+        raise ValueError("the persistent closest point takes interval, affine_fixed or slope_interval; the "
+                         "reference schedule (persistent=False) takes every mode")
     if persistent:
         ws_bytes = L.niq_closest_point_persistent_workspace_size(Q)
         ws = _io.workspace(ws_bytes)
@@ -230,7 +241,8 @@ def closest_point(func, params, lower, upper, query_points, eps=0.001, batch_pro
         B = int(batch_process_size)
         cap = max(Q + 2 * B, 1 << 16)
         while True:
-            ws_bytes = L.niq_closest_point_workspace_size(Q, B, cap)
+            ws_bytes = (L.niq_closest_point_growing_workspace_size(m.handle, _lib.C.byref(bo), Q, B, cap)
+                        if func.mode in GROWING_MODES else L.niq_closest_point_workspace_size(Q, B, cap))
             ws = t.empty(ws_bytes, dtype=t.uint8, device='cuda')
             try:
                 _lib.check(L.niq_closest_point(m.handle, _lib.C.byref(bo), _host3(lower), _host3(upper), Q,

@@ -57,7 +57,7 @@ def main():
     ap.add_argument('--reference', default=os.environ.get('NIQ_REFERENCE'),
                     help='root of the reference checkout (default: $NIQ_REFERENCE)')
     ap.add_argument('--only', default=None,
-                    help='write one fixture only: frustum, camera, mc, samples')
+                    help='write one fixture only: frustum, camera, mc, samples, tree_growing')
     args = ap.parse_args()
     if not args.reference or not os.path.isdir(os.path.join(args.reference, 'src')):
         ap.error('--reference (or NIQ_REFERENCE) must name the reference checkout')
@@ -87,6 +87,9 @@ def main():
         return
     if args.only == 'mc':
         mc_fixture(extract_cell)
+        return
+    if args.only == 'tree_growing':
+        tree_growing_fixture(kd_tree, load_as_reference, models)
         return
     if args.only == 'samples':
         samples_fixture(args.reference, affine, slope_interval, queries, kd_tree, load_as_reference, t0)
@@ -253,6 +256,45 @@ def frustum_fixture(queries, load_as_reference, models, t0):
         print(f'frustum {name} {time.time() - t0:.1f}s', flush=True)
     out['frustum/cam'] = np.concatenate([eye, look, up, left, [40., 30., 12, 10]]).astype(np.float32)
     np.savez_compressed(os.path.join(HERE, 'frustum.npz'), **out)
+
+
+def tree_growing_fixture(kd_tree, load_as_reference, models):
+    """construct_uniform_unknown_levelset_tree (src/kd_tree.py:19-218) in the growing-term
+    modes on the 3x32x3 ReLU model, 8 bisections: affine_truncate with 8 and 64 terms,
+    affine_append with 4, affine_all; and closest_point in affine_truncate (8 and 64
+    terms) on the fitted sphere model of queries.npz."""
+    import jax.numpy as jnp
+    out = {}
+    params = models['relu32x3']
+    out.update(flat('model/relu32x3', params))
+    lower, upper = jnp.array((-1., -1., -1.)), jnp.array((1., 1., 1.))
+    cases = {'truncate8': ('affine_truncate', {'affine_n_truncate': 8, 'affine_truncate_policy': 'absolute'}),
+             'truncate64': ('affine_truncate', {'affine_n_truncate': 64, 'affine_truncate_policy': 'absolute'}),
+             'append4': ('affine_append', {'affine_n_append': 4}),
+             'all': ('affine_all', {})}
+    for name, (mode, kw) in cases.items():
+        f, p = load_as_reference(params, 'relu32x3', mode, **kw)
+        d = kd_tree.construct_uniform_unknown_levelset_tree(f, p, lower, upper, split_depth=8,
+                                                            with_interior_nodes=True, with_exterior_nodes=True)
+        for kind in ('unknown', 'interior', 'exterior'):
+            valid = np.asarray(d[f'{kind}_node_valid'])
+            out[f'tree/{name}/{kind}/lower'] = np.asarray(d[f'{kind}_node_lower'])[valid]
+            out[f'tree/{name}/{kind}/upper'] = np.asarray(d[f'{kind}_node_upper'])[valid]
+        print(f'tree {name}', flush=True)
+    gq = dict(np.load(os.path.join(HERE, 'queries.npz')))
+    A = {k[len('model/A/'):]: v for k, v in gq.items() if k.startswith('model/A/')}
+    out.update(flat('model/A', A))
+    q = gq['cp/q']
+    out['cp/q'] = q
+    for name in ('truncate8', 'truncate64'):
+        mode, kw = cases[name]
+        f, p = load_as_reference(A, 'A', mode, **kw)
+        for B_ in (8, 2048):
+            dist, loc = kd_tree.closest_point(f, p, lower, upper, jnp.array(q), eps=0.05, batch_process_size=B_)
+            out[f'cp/{name}/B{B_}/dist'] = np.asarray(dist)
+            out[f'cp/{name}/B{B_}/loc'] = np.asarray(loc)
+            print(f'cp {name} B{B_}', flush=True)
+    np.savez_compressed(os.path.join(HERE, 'tree_growing.npz'), **out)
 
 
 def camera_fixture():

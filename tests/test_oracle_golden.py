@@ -217,3 +217,31 @@ def test_c_marching_cubes_matches_numpy_oracle(R):
     assert tris.shape == ref.shape and tris.shape[0] > 500
     np.testing.assert_allclose(tris, ref, atol=1e-5)
     assert cpu_tree.hmc_leaves(layers, leaves, want_tris=False) == tris.shape[0]
+
+
+@pytest.mark.parametrize('name,mode,kw', [('truncate8', 'affine_truncate', {'affine_n_truncate': 8}),
+                                          ('truncate64', 'affine_truncate', {'affine_n_truncate': 64}),
+                                          ('append4', 'affine_append', {'affine_n_append': 4}),
+                                          ('all', 'affine_all', {})])
+def test_levelset_tree_growing_modes(R, name, mode, kw):
+    """The oracle's tree in the growing-term modes against the reference's, box for box
+    and in the same order."""
+    g = golden('tree_growing.npz')
+    params = model_from(g, 'model/relu32x3')
+    f = R.generate_implicit(params, mode, **kw)
+    d = R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=8,
+                                                  with_interior_nodes=True, with_exterior_nodes=True)
+    for kind in ('unknown', 'interior', 'exterior'):
+        np.testing.assert_array_equal(d[f'{kind}_node_lower'], g[f'tree/{name}/{kind}/lower'])
+        np.testing.assert_array_equal(d[f'{kind}_node_upper'], g[f'tree/{name}/{kind}/upper'])
+
+
+@pytest.mark.parametrize('name,K', [('truncate8', 8), ('truncate64', 64)])
+def test_closest_point_truncate(R, name, K):
+    """The oracle's closest point in affine_truncate against the reference's."""
+    g = golden('tree_growing.npz')
+    A = model_from(g, 'model/A')
+    f = R.generate_implicit(A, 'affine_truncate', affine_n_truncate=K)
+    for B in (8, 2048):
+        d, _ = R.closest_point(f, A, -np.ones(3), np.ones(3), g['cp/q'], eps=0.05, batch_process_size=B)
+        np.testing.assert_allclose(d, g[f'cp/{name}/B{B}/dist'], rtol=1e-5, atol=1e-6)
