@@ -14,9 +14,14 @@ per level, the reference's loop structure) is measured beside it.
 Multi-GPU: the path has no exchange step, so N GPUs run N independent replicas of the
 workload (torchrun, one rank per GPU); value = all ranks' boxes / max-over-ranks time.
 
---impl reference times the NumPy restatement of the reference's algorithm (oracle/,
-the reference itself is JAX and cannot run here) on the host cores: each step builds
-the same tree to 15 bisections (a bounded sample of the workload) and reports boxes/s.
+The default line also carries the plain-method ray cast at its stated size
+(``rays_plain_method``: 128^2 rays, persistent vs plain, end to end and roofline) and a
+bounded sample of the precision workload (``precision_sample``: 3xTF32 tensor-core vs FP32
+products at 256 noise terms); ``--no-extras`` leaves them out.
+
+--impl reference times the oracle's C/OpenMP restatement of the reference's algorithm
+(oracle/cpu_tree.c; the reference itself is JAX and cannot run here) on all host cores:
+each step builds the same 24-bisection tree and runs marching cubes on its leaves.
 """
 from __future__ import annotations
 
@@ -139,6 +144,10 @@ def run_ours(args):
     model = niq.mlp.device_model(params)
     L = lib.load()
     bo = f.bound_opts()
+    eng = lib.C.c_int32(-1)
+    lib.check(L.niq_tree_engine(model.handle, lib.C.byref(bo), lib.C.byref(eng)))
+    tree_engine = {0: "fp32 tile engine (k_tree)", 1: "tensor cores, 3xTF32 hidden layers (k_tree_tc)",
+                   2: "growing-term engine"}[eng.value]
     stream = torch.cuda.current_stream()
     l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')  # 256 MiB > 129 MB L2
 
@@ -249,19 +258,16 @@ def run_ours(args):
     value = replica_rate(n_boxes, t_step, world)
     bf = box_flops(params)
     t_tree = sum(tree_t) / len(tree_t)
-    achieved_tf = n_boxes * bf / t_tree / 1e12
-    sm_max = measured_peaks().get('sm_max_mhz', 2070.0)
-    props = torch.cuda.get_device_properties(local)
-    fp32_peak = fp32_peak_tflops(local)
     line = {
         "metric": "bounded boxes/s (level-set tree 256^3 + HMC, 12-sphere ReLU 3x64x4 MLP, affine_fixed)",
         "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (fitted 12-sphere SDF MLP, committed weights)",
-        "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12", "split_depth": args.split_depth,
-                   "leaves": int(counts_host[0]), "boxes_per_step": n_boxes, "triangles_per_step": n_tris,
-                   "mode": "affine_fixed conservative", "l2": "flushed: 256 MiB write between timed steps",
-                   "parallelism": f"replicas x{world}"},
+        "config": dict(WORKLOAD_CONFIG, split_depth=args.split_depth, parallelism=f"replicas x{world}"),
+        "details": {"leaves": int(counts_host[0]), "boxes_per_step": n_boxes, "triangles_per_step": n_tris,
+                    "arithmetic": "affine_fixed with outward rounding (every bound conservative)",
+                    "tree_engine": tree_engine,
+                    "l2": "flushed: 256 MiB write between timed steps"},
         "e2e": {"value": replica_rate(n_boxes, t_e2e, world), "unit": "boxes/s", "h2d_bytes_per_step": 24,
                 "d2h_bytes_per_step": int(out.nbytes) + 32, "ms_per_step": t_e2e * 1e3,
                 "api": "kd_tree.hierarchical_marching_cubes(depth=8, n_subcell_depth=0)"},
@@ -274,22 +280,13 @@ def run_ours(args):
                     "(niq_levelset_tree_batches)",
             "persistent_speedup": t_batch / (sum(tree_t) / len(tree_t))},
         "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3},
-        "roofline": {"bound": "fp32", "kernel": "k_tree (persistent level-set tree)",
-                     "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak,
-                     # DRAM bytes of one k_tree launch: an ncu capture of the 18-bisection tree
-                     # (148.5 KB read + 6.9 KB written for 332,953 boxes) scaled by boxes
-                     "traffic": (148480 + 6912) / 332953 * n_boxes,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the "
-                                       "18-bisection tree, scaled to this launch's boxes; the level arrays stay in L2",
-                     "flops_per_box": bf,
-                     "peak_source": (f"FP32 FMA pipe: {props.multi_processor_count} SMs x 128 lanes x 2 FLOP x "
-                                     f"{sm_max:.0f} MHz (MEASURED_PEAKS.json sm_max_mhz); the file has no FP32 "
-                                     "figure and this kernel uses neither tensor cores nor significant HBM"),
-                     "hbm_gbs_of_measured": None},
+        "roofline": tree_roofline(eng.value, n_boxes, bf, t_tree, params, local),
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0 and not args.no_extras:
+        line["rays_plain_method"] = rays_plain_method(niq, args.steps, args.warmup, l2buf)
+        line["precision_sample"] = precision_sample(niq, args.steps, args.warmup)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(params)
         print(json.dumps(line))
@@ -297,20 +294,197 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(params, seconds=20.0, depth=CPU_DEPTH):
-    """The oracle's C/OpenMP restatement of the tree (oracle/cpu_tree.c, float32, the
-    reference's arithmetic) on every host core, building the level-set tree of the same
-    model to ``depth`` bisections (the full 256^3 tree at 24), repeated for up to
-    ``seconds``; the NumPy oracle's rate on a 15-bisection tree is reported beside it."""
+# DRAM bytes per classified box of the tree kernels (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch on the 24-bisection tree of the 12-sphere model,
+# divided by its boxes): the level arrays stay in L2, so a box costs well under its 24 B
+# of node I/O.  Keyed by the engine code of niq_tree_engine.
+TREE_DRAM_BYTES_PER_BOX = {0: (148480 + 6912) / 332953}
+
+
+def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
+    """Roofline of the tree kernel: algorithmic FLOPs (2 (v + 2) S per box) over the
+    tree phase's CUDA-event time.  The FP32 engine is bound by the FP32 FMA pipe; the
+    tensor-core engine executes the four signed rows of every hidden layer as 3 tf32
+    products per FLOP on the tensor pipe (dense tf32 peak = half the measured bf16 burst)
+    and the err row and the linearisations on the FP32 pipe, so both fractions are given."""
+    hidden = sum(A.shape[0] * A.shape[1] for A, _, _ in importlib.import_module(PKG).mlp.spec_layers(params)[1:-1])
+    achieved = n_boxes * bf / t_tree / 1e12
+    fp32_peak = fp32_peak_tflops(device)
+    tf32_peak = measured_peaks().get('bf16_tflops', 1900.) / 2
+    per_box = TREE_DRAM_BYTES_PER_BOX.get(engine)
+    out = {"kernel": "k_tree_tc (persistent level-set tree, tensor cores)" if engine == 1
+           else "k_tree (persistent level-set tree)",
+           "achieved": achieved, "unit": "TFLOP/s", "flops_per_box": bf,
+           "traffic": per_box * n_boxes if per_box is not None else None,
+           "traffic_source": "ncu dram bytes per box of the same kernel on the 24-bisection tree" if per_box
+           else "not captured for this kernel"}
+    if engine == 1:
+        tensor = n_boxes * 3 * 2 * 4 * hidden / t_tree / 1e12
+        out.update({"bound": "tensor", "peak": tf32_peak, "frac": achieved / tf32_peak,
+                    "tensor_pipe_tflops": tensor, "tensor_pipe_frac": tensor / tf32_peak,
+                    "fp32_peak": fp32_peak, "frac_of_fp32_peak": achieved / fp32_peak,
+                    "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json); FP32 FMA "
+                                   "pipe: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock"})
+    else:
+        out.update({"bound": "fp32", "peak": fp32_peak, "frac": achieved / fp32_peak,
+                    "peak_source": "FP32 FMA pipe: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock "
+                                   "(MEASURED_PEAKS.json has no FP32 figure)"})
+    return out
+
+
+def rays_plain_method(niq, steps, warmup, l2buf):
+    """The plain-method workload at its stated size: 128 x 128 rays of the 3->32x3->1 ReLU
+    model (He-normal seed 0, median-biased), affine_fixed with outward rounding, 64 steps,
+    eye at distance 3 aimed at the origin, 60 degree field of view.  Persistent (one
+    launch) and plain (one launch + host compaction per iteration) forms with the rays
+    resident on the device, and end to end through queries.cast_rays with host arrays in
+    and out.  Roofline: 10 S FLOP per ray-step (one v = 1 segment bound, 6 S, and two
+    point evaluations, 4 S; S = 2,176 MACs) against the FP32 FMA peak."""
+    import torch
+    params = niq.workloads.plain_small_model()
+    f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=True)
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    eye = np.array([0., 0., 3.], np.float32)
+    look, up, _ = niq.render.look_at(eye)
+    roots, dirs = niq.render.generate_camera_rays(eye, look, up, res=128, fov_deg=60.)
+    rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
+    n = roots.shape[0]
+    stream = torch.cuda.current_stream()
+    out = {}
+    for form, persistent in (("persistent", True), ("plain", False)):
+        for _ in range(warmup):
+            r = niq.queries.cast_rays((f,), (params,), rt, dt, opts, persistent=persistent, return_device=True)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            flush_l2(l2buf)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = niq.queries.cast_rays((f,), (params,), rt, dt, opts, persistent=persistent, return_device=True)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        t = sum(ts) / len(ts)
+        out[form] = {"value": n / t, "unit": "rays/s", "ms_per_step": t * 1e3,
+                     "ray_steps": int(r[2].sum().item()), "hits": int((r[1] > 0).sum().item())}
+    # end to end: host roots/dirs in, host t/hit_id/count out, every step
+    for _ in range(warmup):
+        niq.queries.cast_rays((f,), (params,), roots, dirs, opts)
+    ts = []
+    for _ in range(steps):
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t_, hid, cnt, _ = niq.queries.cast_rays((f,), (params,), roots, dirs, opts)
+        ts.append(time.perf_counter() - t0)
+    te = sum(ts) / len(ts)
+    macs = mlp_macs(params)
+    fl = 10 * macs * out["persistent"]["ray_steps"]
+    peak = fp32_peak_tflops(torch.cuda.current_device())
+    ach = fl / (out["persistent"]["ms_per_step"] * 1e-3) / 1e12
+    out["persistent"]["e2e"] = {"value": n / te, "unit": "rays/s", "ms_per_step": te * 1e3,
+                                "h2d_bytes_per_step": int(roots.nbytes + dirs.nbytes),
+                                "d2h_bytes_per_step": int(t_.nbytes + hid.nbytes + cnt.nbytes + 8),
+                                "api": "queries.cast_rays (numpy in, numpy out)"}
+    out["persistent"]["roofline"] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                                     "frac": ach / peak, "flops_per_ray_step": 10 * macs}
+    out["persistent_vs_plain"] = out["plain"]["ms_per_step"] / out["persistent"]["ms_per_step"]
+    out["config"] = {"workload": "cast_rays_plain_method", "model": "relu 3-32x3-1 he-normal seed 0",
+                     "rays": n, "n_max_step": 64, "mode": "affine_fixed conservative",
+                     "l2": "flushed between timed steps"}
+    return out
+
+
+def precision_sample(niq, steps, warmup):
+    """The precision workload on a bounded sample: ReLU 3->256x8->1 (seed 7, median-biased),
+    affine_truncate with 256 noise terms, conservative, the 3xTF32 tensor-core products
+    against FP32 FMA.  1024 boxes of half-width 0.01 are classified per form, and an 8x8
+    strided sample of the 1024x1024 ray image (every 128th ray per axis) is cast: a
+    segment costs about 237 MFLOP at 256 terms, so the full image takes minutes.
+    Roofline of the tensor-core classification: 3 tf32 products per algorithmic FLOP
+    against the dense tf32 peak (half the measured bf16 burst)."""
+    import torch
+    params = niq.workloads.precision_model()
+    eye = np.array([0., 0., 3.], np.float32)
+    look, up, _ = niq.render.look_at(eye)
+    roots, dirs = niq.render.generate_camera_rays(eye, look, up, res=1024, fov_deg=60.)
+    sub = (np.arange(0, 1024, 128)[:, None] * 1024 + np.arange(0, 1024, 128)[None, :]).reshape(-1)
+    rs, ds = torch.from_numpy(roots[sub]).cuda(), torch.from_numpy(dirs[sub]).cuda()
+    opts = niq.queries.get_default_cast_opts()
+    dims = [(A.shape[0], A.shape[1], act) for A, _, act in niq.mlp.spec_layers(params)]
+    fl, rows = 0, 3
+    for i, o, act in dims:
+        fl += 2 * (rows + 2) * i * o
+        if act != 'none':
+            rows = min(rows + o, 256)
+    rng = np.random.default_rng(3)
+    nb = 1024
+    c = torch.from_numpy(rng.uniform(-0.8, 0.8, (nb, 3)).astype(np.float32)).cuda()
+    vv = torch.from_numpy(np.tile((0.01 * np.eye(3, dtype=np.float32))[None], (nb, 1, 1))).cuda()
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            r = fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return r, sum(ts) / len(ts)
+    out = {}
+    for name, products in (("3xtf32", "3xtf32"), ("fp32", "fp32")):
+        f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_truncate', conservative=True,
+                                                                    products=products, affine_n_truncate=256)
+        _, tb = timed(lambda: f.bounds_general_box(params, c, vv), max(1, steps // 4), 1)
+        r, tr = timed(lambda: niq.queries.cast_rays((f,), (params,), rs, ds, opts, return_device=True), 1, 1)
+        out[name] = {"boxes_per_s": nb / tb, "classify_ms": tb * 1e3, "rays_per_s": rs.shape[0] / tr,
+                     "cast_ms": tr * 1e3, "ray_steps": int(r[2].sum().item()),
+                     "achieved_tflops": nb * fl / tb / 1e12}
+    tf32_peak = measured_peaks().get('bf16_tflops', 1900.) / 2
+    a3 = 3 * out["3xtf32"]["achieved_tflops"]
+    out["3xtf32"]["roofline"] = {"bound": "tensor", "achieved": a3, "peak": tf32_peak, "unit": "TFLOP/s",
+                                 "frac": a3 / tf32_peak,
+                                 "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json)"}
+    out["tensor_vs_fp32"] = {"boxes": out["3xtf32"]["boxes_per_s"] / out["fp32"]["boxes_per_s"],
+                             "rays": out["3xtf32"]["rays_per_s"] / out["fp32"]["rays_per_s"]}
+    out["config"] = {"workload": "precision_relu256x8_truncate256", "boxes": nb, "rays": int(rs.shape[0]),
+                     "flop_per_box": fl, "sample": "8x8 strided rays of the 1024x1024 image"}
+    return out
+
+
+WORKLOAD_CONFIG = {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12", "split_depth": SPLIT_DEPTH,
+                   "hmc": "marching cubes on every unknown leaf (depth 8, n_subcell_depth 0)"}
+
+
+def cpu_tree_hmc_step(layers, depth, cores):
+    """One step of the workload on the host cores through the oracle's C/OpenMP
+    restatement (oracle/cpu_tree.c): the level-set tree to ``depth`` bisections in the
+    reference's arithmetic, then marching cubes on every unknown leaf.  Returns
+    (boxes classified, triangles)."""
     from oracle import cpu_tree
+    _, nb, leaves = cpu_tree.levelset_tree(layers, -np.ones(3), np.ones(3), depth, threads=cores, want_leaves=True)
+    tris = cpu_tree.hmc_leaves(layers, leaves, threads=cores)
+    return nb, tris.shape[0]
+
+
+def cpu_baseline(params, seconds=20.0, depth=CPU_DEPTH):
+    """The oracle's C/OpenMP restatement (oracle/cpu_tree.c, float32, the reference's
+    arithmetic) on every host core: the same tree + marching-cubes step, repeated for up
+    to ``seconds`` (at most 3 times); the NumPy oracle's rate on a 15-bisection tree is
+    reported beside it."""
     from oracle import ref_np as R
     niq = importlib.import_module(PKG)
     layers = niq.mlp.spec_layers(params)
     cores = os.cpu_count()
     t0 = time.perf_counter()
-    boxes, reps = 0, 0
+    boxes, reps, ntri = 0, 0, 0
     while True:
-        _, nb, _ = cpu_tree.levelset_tree(layers, -np.ones(3), np.ones(3), depth, threads=cores)
+        nb, ntri = cpu_tree_hmc_step(layers, depth, cores)
         boxes += nb
         reps += 1
         if time.perf_counter() - t0 > seconds or reps >= 3:
@@ -321,8 +495,9 @@ def cpu_baseline(params, seconds=20.0, depth=CPU_DEPTH):
     d = R.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=15)
     np_rate = d['n_boxes_classified'] / (time.perf_counter() - t1)
     return {"value": boxes / dt, "unit": "boxes/s", "cores": cores, "kind": "port",
-            "sample": f"oracle/cpu_tree.c (C, OpenMP on {cores} threads) level-set tree of the same model to "
-                      f"{depth} bisections ({boxes // reps} boxes) x{reps}; the tree without the HMC phase",
+            "sample": f"oracle/cpu_tree.c (C, OpenMP on {cores} threads): level-set tree of the same model to "
+                      f"{depth} bisections ({boxes // reps} boxes) and marching cubes on its leaves ({ntri} "
+                      f"triangles), x{reps}",
             "numpy_oracle_boxes_per_s": np_rate}
 
 
@@ -331,17 +506,16 @@ def run_reference(args):
     if rank != 0:
         return
     niq = importlib.import_module(PKG)
-    from oracle import cpu_tree
     params = niq.workloads.spheres_sdf_model()
     layers = niq.mlp.spec_layers(params)
     cores = os.cpu_count()
     depth = CPU_DEPTH
     for _ in range(args.warmup):
-        cpu_tree.levelset_tree(layers, -np.ones(3), np.ones(3), depth - 6, threads=cores)
-    times, boxes = [], 0
+        cpu_tree_hmc_step(layers, depth - 6, cores)
+    times, boxes, ntri = [], 0, 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, boxes, _ = cpu_tree.levelset_tree(layers, -np.ones(3), np.ones(3), depth, threads=cores)
+        boxes, ntri = cpu_tree_hmc_step(layers, depth, cores)
         times.append(time.perf_counter() - t0)
     t = sum(times) / len(times)
     v = boxes / t
@@ -350,13 +524,14 @@ def run_reference(args):
             "value": v, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (fitted 12-sphere SDF MLP, committed weights)",
-            "config": {"workload": "levelset_tree_hmc", "model": "relu 3-64x4-1 spheres12",
-                       "split_depth": depth, "boxes_per_step": int(boxes),
-                       "note": "the reference is JAX, which is absent; the oracle's C/OpenMP restatement of its "
-                               "tree runs on the host cores (tree only, no HMC)"},
+            "config": dict(WORKLOAD_CONFIG, parallelism=f"replicas x{world}"),
+            "details": {"boxes_per_step": int(boxes), "triangles_per_step": int(ntri), "host_cores": cores,
+                        "arithmetic": "the reference's: float32, round to nearest, no outward rounding",
+                        "note": "the reference is JAX, which is absent; the oracle's C/OpenMP restatement of its "
+                                "tree and marching cubes runs on the host cores"},
             "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": cores, "kind": "port",
-                             "sample": f"oracle/cpu_tree.c tree to {depth} bisections ({boxes} boxes), "
-                                       f"OpenMP on {cores} threads"},
+                             "sample": f"oracle/cpu_tree.c tree to {depth} bisections ({boxes} boxes) + marching "
+                                       f"cubes ({ntri} triangles), OpenMP on {cores} threads"},
             "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -686,6 +861,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--split-depth', type=int, default=SPLIT_DEPTH, help='bisections of the tree (24: 256^3 leaves)')
     ap.add_argument('--quick', action='store_true', help='timed steps only (for profiler runs)')
+    ap.add_argument('--no-extras', action='store_true',
+                    help='skip the plain-method ray cast and the precision sample in the default line')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == 'ours' else args.warmup
     if args.impl == 'reference':
