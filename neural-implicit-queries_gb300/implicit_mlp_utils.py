@@ -10,16 +10,18 @@ from .slope_interval import SlopeIntervalImplicitFunction
 def generate_implicit_from_params(params, mode, **kwargs):
     """The mode switch of src/implicit_mlp_utils.py:23-64 for an in-memory spec.
     Extra keywords: ``conservative`` (default True) selects outward rounding;
-    ``products`` ('auto', 'fp32', '3xtf32') how the affine_truncate/affine_all modes form
-    their dense products."""
+    ``products`` ('auto', 'fp32', '3xtf32') how dense products are formed where there is a
+    choice: the affine_truncate/affine_all engine, and the affine_fixed level-set tree
+    (tensor cores by default on models of hidden width <= 64; 'fp32' keeps the FP32 tile
+    engine)."""
     cons = kwargs.get('conservative', True)
     prod = kwargs.get('products', 'auto')
     if mode == 'sdf':
         return WeakSDFImplicitFunction(lipschitz_bound=kwargs.get('sdf_lipschitz', 1.)), params
     if mode == 'interval':
-        return AffineImplicitFunction(None, AffineContext('interval'), cons), params
+        return AffineImplicitFunction(None, AffineContext('interval'), cons, prod), params
     if mode == 'affine_fixed':
-        return AffineImplicitFunction(None, AffineContext('affine_fixed'), cons), params
+        return AffineImplicitFunction(None, AffineContext('affine_fixed'), cons, prod), params
     if mode == 'affine_truncate':
         ctx = AffineContext('affine_truncate', truncate_count=kwargs['affine_n_truncate'],
                             truncate_policy=kwargs.get('affine_truncate_policy', 'absolute'))
