@@ -406,6 +406,57 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models,
                               int32_t* status_out,
                               void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- serving: continuous batching of mixed requests ---------------------------------
+ * No counterpart in the reference (it has no server; its queries are called one at a
+ * time).  A server owns n_lanes lanes: a lane is a host worker thread with its own CUDA
+ * stream and lane_scratch_bytes of device scratch, allocated once by niq_server_create,
+ * so submitting and running requests allocates nothing.  niq_batch_submit cuts a request
+ * into slices -- ray tiles of at most slice_rays rays, closest-point slices of at most
+ * slice_queries queries, one slice per intersection -- queues them and returns a ticket
+ * at once.  Free lanes take ray tiles first, then the other slices, and run each on
+ * their stream, so requests that arrive while others run overlap them on the device and
+ * a short ray tile never waits behind a long closest-point batch.  niq_batch_poll
+ * reports, without blocking, whether a request is done and its status (NIQ_OK,
+ * NIQ_ERR_TIMEOUT when a closest-point query spent its node budget -- every result is
+ * still written, an upper bound -- or another error); niq_batch_wait blocks up to a
+ * timeout.  A done ticket is reported once.  Inputs and outputs are the caller's device
+ * arrays and must stay valid until the request is done; models are borrowed. */
+#define NIQ_REQ_RAYS       0   /* queries.cast_rays (src/queries.py:134-175) on a tile      */
+#define NIQ_REQ_CLOSEST    1   /* kd_tree.closest_point (src/kd_tree.py:766-802), persistent */
+#define NIQ_REQ_INTERSECT  2   /* kd_tree.find_any_intersection (src/kd_tree.py:567-655)   */
+typedef struct niq_request {
+    int32_t kind;                 /* NIQ_REQ_*                                              */
+    const niq_model* model;       /* the model (intersection: model A)                      */
+    const niq_model* model_b;     /* intersection: model B                                  */
+    niq_bound_opts opts;
+    niq_cast_opts cast;           /* rays                                                   */
+    int64_t n;                    /* rays or query points                                   */
+    const float* in0;             /* rays: roots (n,3); closest point: points (n,3)         */
+    const float* in1;             /* rays: dirs (n,3)                                       */
+    float* out_f;                 /* rays: t (n); closest point: distance (n)              */
+    float* out_f2;                /* closest point: location (n,3); intersection: loc (3)  */
+    int32_t* out_i;               /* rays: hit_id (n); intersection: found (1)             */
+    int32_t* out_i2;              /* rays: count (n)                                        */
+    float eps;                    /* closest point and intersection                         */
+    int64_t node_budget;          /* closest point: nodes per query (<= 0: none)            */
+    int64_t node_capacity;        /* intersection: nodes per level (<= 0: 2^20)             */
+    float lower[3], upper[3];     /* root box of closest point and intersection             */
+} niq_request;
+typedef struct niq_server_opts {
+    int32_t n_lanes;
+    int64_t slice_rays;
+    int64_t slice_queries;
+    int64_t lane_scratch_bytes;
+} niq_server_opts;
+typedef struct niq_server niq_server;
+int niq_server_create(const niq_server_opts* opts, niq_server** out);
+/* Finishes the queued work, stops the lanes and frees their scratch. */
+int niq_server_destroy(niq_server* server);
+int niq_batch_submit(niq_server* server, const niq_request* request, int64_t* ticket_out);
+int niq_batch_poll(niq_server* server, int64_t ticket, int32_t* done_out, int32_t* status_out);
+int niq_batch_wait(niq_server* server, int64_t ticket, double timeout_s, int32_t* status_out);
+int niq_server_stats(niq_server* server, int64_t* completed, int64_t* in_flight);
+
 #ifdef __cplusplus
 }
 #endif

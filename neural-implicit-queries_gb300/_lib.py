@@ -55,6 +55,21 @@ class CastOpts(C.Structure):
                 ('interval_init_size', C.c_float)]
 
 
+class Request(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('model', C.c_void_p), ('model_b', C.c_void_p), ('opts', BoundOpts),
+                ('cast', CastOpts), ('n', C.c_int64), ('in0', C.c_void_p), ('in1', C.c_void_p),
+                ('out_f', C.c_void_p), ('out_f2', C.c_void_p), ('out_i', C.c_void_p), ('out_i2', C.c_void_p),
+                ('eps', C.c_float), ('node_budget', C.c_int64), ('node_capacity', C.c_int64),
+                ('lower', C.c_float * 3), ('upper', C.c_float * 3)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [('n_lanes', C.c_int32), ('slice_rays', C.c_int64), ('slice_queries', C.c_int64),
+                ('lane_scratch_bytes', C.c_int64)]
+
+
+NIQ_REQ_RAYS, NIQ_REQ_CLOSEST, NIQ_REQ_INTERSECT = 0, 1, 2
+
 _P = C.c_void_p
 _I32, _I64, _F32, _SZ = C.c_int32, C.c_int64, C.c_float, C.c_size_t
 _PF = C.POINTER(C.c_float)
@@ -96,6 +111,12 @@ _SIGS = {
                                             _P, _P, _SZ, _P]),
     'niq_tree_result': (C.c_int, [_P, _I64, _I32, _I32, C.POINTER(_P), C.POINTER(_P)]),
     'niq_tree_engine': (C.c_int, [_P, C.POINTER(BoundOpts), C.POINTER(_I32)]),
+    'niq_server_create': (C.c_int, [C.POINTER(ServerOpts), C.POINTER(_P)]),
+    'niq_server_destroy': (C.c_int, [_P]),
+    'niq_batch_submit': (C.c_int, [_P, C.POINTER(Request), C.POINTER(_I64)]),
+    'niq_batch_poll': (C.c_int, [_P, _I64, C.POINTER(_I32), C.POINTER(_I32)]),
+    'niq_batch_wait': (C.c_int, [_P, _I64, C.c_double, C.POINTER(_I32)]),
+    'niq_server_stats': (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
     'niq_tree_growing_workspace_size': (_SZ, [_P, C.POINTER(BoundOpts), _I64, _I32]),
     'niq_levelset_tree_growing': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
                                             _SZ, _P]),

@@ -347,3 +347,152 @@ class Server:
             self._lock.notify_all()
         for p, r in zip(pend, results):
             p.future.set_result(r)
+
+
+class NativeServer:
+    """The same request kinds served by the library's native runtime (niq_server_create,
+    niq_batch_submit / niq_batch_poll in include/niq.h): lanes of worker threads with their
+    own CUDA streams and pre-allocated scratch take slices of the requests -- ray tiles of
+    ``slice_rays`` rays first, closest-point slices of ``slice_queries`` queries and
+    intersections after them -- as they free up.  ``submit`` returns a Future; a
+    completion thread polls the tickets and copies the results to the host."""
+
+    def __init__(self, params_list, mode='affine_fixed', n_lanes=4, slice_rays=16384, slice_queries=1024,
+                 lane_scratch_bytes=512 << 20, lower=(-1., -1., -1.), upper=(1., 1., 1.), conservative=True):
+        import torch
+        self.torch = torch
+        self.params = list(params_list)
+        self.func, _ = generate_implicit_from_params(self.params[0], mode, conservative=conservative)
+        self.models = [device_model(p) for p in self.params]
+        self.lower = np.asarray(lower, np.float32)
+        self.upper = np.asarray(upper, np.float32)
+        self.L = _lib.load()
+        so = _lib.ServerOpts(int(n_lanes), int(slice_rays), int(slice_queries), int(lane_scratch_bytes))
+        h = _lib.C.c_void_p()
+        _lib.check(self.L.niq_server_create(_lib.C.byref(so), _lib.C.byref(h)))
+        self.handle = h
+        self._lock = threading.Condition()
+        self._pending = {}
+        self._stop = False
+        self.latencies = []
+        self.kind_latencies = collections.defaultdict(list)
+        self.completed = 0
+        self.budget_exhausted = 0
+        self._device = torch.cuda.current_device()
+        self._done = threading.Thread(target=self._complete, daemon=True)
+        self._done.start()
+
+    def _request(self, kind, model):
+        r = _lib.Request()
+        r.kind = kind
+        r.model = model.handle.value
+        r.opts = self.func.bound_opts()
+        r.lower = (_lib.C.c_float * 3)(*self.lower.tolist())
+        r.upper = (_lib.C.c_float * 3)(*self.upper.tolist())
+        return r
+
+    def submit(self, req):
+        """Queue a RayRequest, ClosestRequest or IntersectRequest; returns a Future of the
+        results as the Python Server returns them."""
+        torch = self.torch
+        fut = Future()
+        t0 = time.perf_counter()
+        keep = []
+        if isinstance(req, RayRequest):
+            kind = 'rays'
+            opts = req.opts or queries.get_default_cast_opts()
+            roots = torch.from_numpy(np.ascontiguousarray(req.roots, np.float32)).cuda()
+            dirs = torch.from_numpy(np.ascontiguousarray(req.dirs, np.float32)).cuda()
+            n = roots.shape[0]
+            t = torch.empty(n, dtype=torch.float32, device='cuda')
+            hit = torch.empty(n, dtype=torch.int32, device='cuda')
+            cnt = torch.empty(n, dtype=torch.int32, device='cuda')
+            r = self._request(_lib.NIQ_REQ_RAYS, self.models[req.model])
+            r.cast = _lib.cast_opts(opts)
+            r.n, r.in0, r.in1 = n, roots.data_ptr(), dirs.data_ptr()
+            r.out_f, r.out_i, r.out_i2 = t.data_ptr(), hit.data_ptr(), cnt.data_ptr()
+            keep = [roots, dirs]
+            outs = (t, hit, cnt)
+        elif isinstance(req, ClosestRequest):
+            kind = 'closest'
+            q = torch.from_numpy(np.ascontiguousarray(req.points, np.float32)).cuda()
+            n = q.shape[0]
+            dist = torch.empty(n, dtype=torch.float32, device='cuda')
+            loc = torch.empty((n, 3), dtype=torch.float32, device='cuda')
+            r = self._request(_lib.NIQ_REQ_CLOSEST, self.models[req.model])
+            r.n, r.in0, r.out_f, r.out_f2 = n, q.data_ptr(), dist.data_ptr(), loc.data_ptr()
+            r.eps, r.node_budget = float(req.eps), int(req.node_budget or 0)
+            keep = [q]
+            outs = (dist, loc)
+        else:
+            kind = 'intersect'
+            pa = prepend_op(self.params[req.model_a], spatial_transformation())
+            pa['0000.spatial_transformation.R'] = np.asarray(req.R, np.float32)
+            pa['0000.spatial_transformation.t'] = np.asarray(req.t, np.float32)
+            pb = prepend_op(self.params[req.model_b], spatial_transformation())
+            ma, mb = device_model(pa), device_model(pb)
+            found = torch.zeros(1, dtype=torch.int32, device='cuda')
+            loc = torch.empty(3, dtype=torch.float32, device='cuda')
+            r = self._request(_lib.NIQ_REQ_INTERSECT, ma)
+            r.model_b = mb.handle.value
+            r.n, r.eps, r.node_capacity = 1, float(req.eps), 1 << 20
+            r.out_i, r.out_f2 = found.data_ptr(), loc.data_ptr()
+            keep = [ma, mb]
+            outs = (found, loc)
+        # the inputs are on the device before a lane (another stream) reads them
+        torch.cuda.current_stream().synchronize()
+        ticket = _lib.C.c_int64()
+        _lib.check(self.L.niq_batch_submit(self.handle, _lib.C.byref(r), _lib.C.byref(ticket)))
+        with self._lock:
+            self._pending[ticket.value] = (kind, fut, t0, outs, keep)
+            self._lock.notify_all()
+        return fut
+
+    def _complete(self):
+        self.torch.cuda.set_device(self._device)
+        done, status = _lib.C.c_int32(), _lib.C.c_int32()
+        while True:
+            with self._lock:
+                while not self._pending and not self._stop:
+                    self._lock.wait()
+                if self._stop and not self._pending:
+                    return
+                tickets = list(self._pending)
+            finished = []
+            for tk in tickets:
+                _lib.check(self.L.niq_batch_poll(self.handle, tk, _lib.C.byref(done), _lib.C.byref(status)))
+                if done.value:
+                    finished.append((tk, status.value))
+            if not finished:
+                time.sleep(0.0002)
+                continue
+            for tk, st in finished:
+                with self._lock:
+                    kind, fut, t0, outs, _ = self._pending.pop(tk)
+                if st not in (0, _lib.NIQ_ERR_TIMEOUT):
+                    fut.set_exception(_lib.NIQError(st, f"{kind} request failed"))
+                    continue
+                if st == _lib.NIQ_ERR_TIMEOUT:
+                    self.budget_exhausted += 1
+                if kind == 'intersect':
+                    f, loc = outs
+                    found = bool(f.item())
+                    res = (True, 1, 2, loc.cpu().numpy()) if found else (False, 0, 0, loc.cpu().numpy())
+                else:
+                    res = tuple(o.cpu().numpy() for o in outs)
+                now = time.perf_counter()
+                with self._lock:
+                    self.latencies.append(now - t0)
+                    self.kind_latencies[kind].append(now - t0)
+                    self.completed += 1
+                fut.set_result(res)
+
+    def stats(self):
+        return Server.stats(self)
+
+    def close(self):
+        with self._lock:
+            self._stop = True
+            self._lock.notify_all()
+        self._done.join()
+        _lib.check(self.L.niq_server_destroy(self.handle))
