@@ -757,12 +757,13 @@ def run_batched(args):
                       "some_query_spent_budget": budget_hit, "model_generation_s": t_gen}))
 
 
-def make_serving_requests(niq, n, rng, max_res=512, max_points=16384):
+def make_serving_requests(niq, n, rng, max_res=512, max_points=16384, eps=1e-3, node_budget=4096):
     """The serving mix: ray tiles (64^2..max_res^2 from a random camera at distance 3),
-    closest-point batches (1..max_points points, log-uniform, eps 1e-2, at most 128
-    nodes per query: the models are untrained, their bounds loose, and a served answer
-    within its node budget is an upper bound) and pairwise
-    intersection tests under a random rigid transform (eps 2e-2): 45% / 45% / 10%."""
+    closest-point batches (1..max_points points, log-uniform, eps 1e-3, at most
+    ``node_budget`` nodes per query: the models are untrained, their bounds loose, and a
+    query that spends its budget is answered with its best candidate, an upper bound; the
+    bench counts those requests) and pairwise intersection tests under a random rigid
+    transform (eps 2e-2): 45% / 45% / 10%."""
     srv = niq.serve
     reqs = []
     sizes = [s for s in (64, 128, 256, 512) if s <= max_res]
@@ -780,8 +781,8 @@ def make_serving_requests(niq, n, rng, max_res=512, max_points=16384):
             reqs.append(srv.RayRequest(m, roots, dirs, opts))
         elif u < 0.9:
             k = int(np.exp(rng.uniform(0, np.log(max_points))))
-            reqs.append(srv.ClosestRequest(m, rng.uniform(-1.2, 1.2, (k, 3)).astype(np.float32), eps=1e-2,
-                                           node_budget=128))
+            reqs.append(srv.ClosestRequest(m, rng.uniform(-1.2, 1.2, (k, 3)).astype(np.float32), eps=eps,
+                                           node_budget=node_budget))
         else:
             R = niq.workloads.random_rotation(rng)
             reqs.append(srv.IntersectRequest(m, int(rng.integers(64)), R,
@@ -798,7 +799,11 @@ def run_serve(args):
     niq = importlib.import_module(PKG)
     models = niq.workloads.serving_models(64)
     rng = np.random.default_rng(7)
-    srv = niq.serve.Server(models, budget_bytes=40 << 30, n_streams=4)
+    if args.serve_impl == 'native':
+        srv = niq.serve.NativeServer(models, n_lanes=args.serve_lanes, slice_rays=16384, slice_queries=512,
+                                     lane_scratch_bytes=512 << 20)
+    else:
+        srv = niq.serve.Server(models, budget_bytes=40 << 30, n_streams=4)
     # warm up every model once (packing, uploads, kernel attributes)
     warm = make_serving_requests(niq, 16, rng, max_res=64, max_points=64)
     for f in [srv.submit(r) for r in warm]:
@@ -811,16 +816,24 @@ def run_serve(args):
     t_sat = time.perf_counter() - t0
     peak = len(sat) / t_sat
     st_sat = srv.stats()
+    spent_sat = srv.budget_exhausted
     srv.latencies.clear()
     srv.kind_latencies.clear()
     out = {"metric": "served requests/s and p50/p99 latency (64 resident MLPs, mixed requests)",
            "unit": "requests/s", "saturation": {"requests": len(sat), "seconds": t_sat, "req_per_s": peak,
-                                                 "errors": errors, "by_kind": st_sat.get("by_kind")}, "rates": []}
+                                                 "errors": errors, "by_kind": st_sat.get("by_kind"),
+                                                 "closest_requests_budget_spent": spent_sat}, "rates": [],
+           "config": {"workload": "serving_mix", "impl": args.serve_impl, "lanes": args.serve_lanes,
+                      "closest_point": "eps 1e-3, persistent traversal, 4096 nodes per query; a request whose "
+                                       "query spends the budget is answered with upper bounds and counted",
+                      "mix": "45% ray tiles 64^2..512^2, 45% closest-point batches 1..16k points, "
+                             "10% intersections under random rigid transforms"}}
     for frac in args.serve_fracs:
         rate = frac * peak
         reqs = make_serving_requests(niq, max(8, int(rate * args.serve_seconds)), rng, max_res=args.serve_max_res)
         srv.latencies.clear()
         srv.kind_latencies.clear()
+        srv.budget_exhausted = 0
         gaps = rng.exponential(1.0 / rate, len(reqs))
         t_start = time.perf_counter()
         t_next = t_start
@@ -836,7 +849,8 @@ def run_serve(args):
         st = srv.stats()
         out["rates"].append({"fraction_of_peak": frac, "offered_req_per_s": rate, "completed": st.get("completed", 0),
                              "achieved_req_per_s": len(reqs) / t_all, "p50_ms": st.get("p50_ms"),
-                             "p99_ms": st.get("p99_ms"), "errors": errs, "by_kind": st.get("by_kind")})
+                             "p99_ms": st.get("p99_ms"), "errors": errs, "by_kind": st.get("by_kind"),
+                             "closest_requests_budget_spent": srv.budget_exhausted})
     srv.close()
     seventy = [r for r in out["rates"] if abs(r["fraction_of_peak"] - 0.7) < 1e-6]
     out["value"] = peak
@@ -851,6 +865,9 @@ def main():
     ap.add_argument('--serve-seconds', type=float, default=10.0)
     ap.add_argument('--serve-max-res', type=int, default=512)
     ap.add_argument('--serve-fracs', type=float, nargs='+', default=[0.3, 0.5, 0.7, 0.9])
+    ap.add_argument('--serve-impl', default='native', choices=['native', 'python'],
+                    help='the native serving runtime (niq_batch_submit) or the Python scheduler')
+    ap.add_argument('--serve-lanes', type=int, default=8)
     ap.add_argument('--n-models', type=int, default=512)
     ap.add_argument('--plain-models', type=int, default=64)
     ap.add_argument('--node-budget', type=int, default=2048,
