@@ -684,9 +684,11 @@ def camera_ray(look_dir, up_dir, left_dir, fov_x, fov_y, theta_x, theta_y, dtype
     return normalize(p).astype(dtype)
 
 
-def _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32):
+def _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32, near=None):
     """The substep loop of one cast_rays_frustum iteration for a batch of frusta
-    (src/queries.py:202-321): returns (t, step_size, is_hit, hit_id, demands_subd, steps)."""
+    (src/queries.py:202-321): returns (t, step_size, is_hit, hit_id, demands_subd, steps).
+    ``near`` (optional, (n,) bool) is or-ed with the frusta whose box bound or hit test
+    sat within NEAR_REL of its threshold."""
     root, look, up, left, fov_x, fov_y, res_x, res_y = cam
     x_lo, y_lo, x_hi, y_hi = rng_[:, 0], rng_[:, 1], rng_[:, 2], rng_[:, 3]
     single = (x_lo + 1 == x_hi) & (y_lo + 1 == y_hi)
@@ -718,12 +720,20 @@ def _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32):
         center = (root[None, :] + (np.asarray(0.5, f32) * (t + t_adj))[:, None] * mid).astype(f32)
         cvec = ((np.asarray(0.5, f32) * (t_adj - t))[:, None] * mid).astype(f32)
         vecs = np.stack((cvec, right_front, up_front), axis=1)
+        live = ~is_hit
         for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
-            btype = func.classify_general_box(params, center, vecs)
+            if near is not None:
+                blo, bhi, bn = func.bounds_near(params, center, vecs)
+                btype = sign_from_bounds(blo, bhi)
+            else:
+                btype = func.classify_general_box(params, center, vecs)
             can_step &= (btype == SIGN_POSITIVE) | (btype == SIGN_NEGATIVE)
             p0 = (root[None, :] + t[:, None] * mid).astype(f32)
             p1 = (root[None, :] + (t + hit_eps)[:, None] * mid).astype(f32)
-            this_hit = np.sign(func(params, p0)) != np.sign(func(params, p1))
+            v0, v1 = func(params, p0), func(params, p1)
+            if near is not None:
+                near |= live & (bn | value_near(v0, v1))
+            this_hit = np.sign(v0) != np.sign(v1)
             hit_id = np.where(this_hit, fid, hit_id).astype(np.int32)
             is_hit |= this_hit
         this_step = np.where(can_step, size, hit_eps * single.astype(f32)).astype(f32)
@@ -735,13 +745,27 @@ def _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32):
     return t, size, is_hit, hit_id, demands, steps
 
 
-def cast_rays_frustum(funcs, params_list, cam_params, opts):
+def _cmp_near(a, b, rel=NEAR_REL):
+    """True where the comparison a > b sits within rel (relative) of flipping."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b) <= rel * np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-30)
+
+
+def cast_rays_frustum(funcs, params_list, cam_params, opts, trace=False):
     """src/queries.py:178-587: frusta over integer pixel ranges march like rays with a
     3-vector box (the frustum's extent at the far end of the step), split in half along
     the wider axis when the step size falls behind the frustum's width, and hit only as
     single pixels.  Returns (out_t, out_hit_id, out_count, n_frustum_steps) with the
     outputs indexed [x, y] as the reference writes them.  The reference's buckets and
-    compaction do not change any frustum's result; the frusta are kept compact here."""
+    compaction do not change any frustum's result; the frusta are kept compact here.
+
+    With ``trace`` a fifth (res_x, res_y) bool array marks the pixels whose frustum path
+    (the pixel's frustum and every frustum it was split from) took a decision within
+    NEAR_REL of flipping: a box bound or hit test (bounds_near, value_near), the step
+    limit t > max_dist, a refinement comparison of the frustum width with the step, or
+    the truncation of the fractional step count.  Two implementations that differ only
+    by rounding can give a pixel different results only where it is marked."""
     f32 = funcs[0].dtype
     root, look, up, left, fov_x, fov_y, res_x, res_y = cam_params
     cam = (np.asarray(root, f32), np.asarray(look, f32), np.asarray(up, f32), np.asarray(left, f32),
@@ -754,6 +778,7 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts):
     size = (np.ones(ns * ns, f32) * np.asarray(opts['interval_init_size'], f32) *
             np.asarray(opts['max_dist'], f32)).astype(f32)
     count = np.zeros(ns * ns, f32)
+    near = np.zeros(ns * ns, bool)
     fin = []
     it = 0
     n_steps = 0
@@ -761,15 +786,21 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts):
     fov_y_rad = np.asarray(np.deg2rad(np.asarray(fov_y, f32)), f32)
     while rng_.shape[0]:
         n_steps += rng_.shape[0]
-        t, size, is_hit, hit_id, demands, steps = _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32)
+        t, size, is_hit, hit_id, demands, steps = _frust_step(funcs, params_list, cam, rng_, t, size, opts, f32,
+                                                              near if trace else None)
         area = ((rng_[:, 2] - rng_[:, 0]) * (rng_[:, 3] - rng_[:, 1])).astype(np.int64)
         count = (count + steps.astype(f32) * (np.asarray(1., f32) / area.astype(f32))).astype(f32)
         is_hit = is_hit & (area == 1)
         term = is_hit | (t > opts['max_dist']) | (it >= opts['n_max_step'])
+        if trace:
+            near |= _cmp_near(t, opts['max_dist'])
+            frac = count.astype(np.float64) - np.floor(count.astype(np.float64))
+            near |= term & ((frac <= NEAR_REL * np.maximum(count, 1.)) | (1 - frac <= NEAR_REL * np.maximum(count, 1.)))
         if term.any():
-            fin.append((rng_[term], t[term], hit_id[term], count[term]))
+            fin.append((rng_[term], t[term], hit_id[term], count[term], near[term]))
         keep = ~term
         rng_, t, size, count, demands = rng_[keep], t[keep], size[keep], count[keep], demands[keep]
+        near = near[keep]
         it += opts['n_substeps']
         if not rng_.shape[0]:
             break
@@ -780,6 +811,8 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts):
         can = (rng_[:, 2] > rng_[:, 0] + 1) | (rng_[:, 3] > rng_[:, 1] + 1)
         rf = np.asarray(opts['refine_width_fac'], f32)
         refine = ((wx > rf * size) | (wy > rf * size) | demands) & can
+        if trace:
+            near |= can & ~demands & (_cmp_near(wx, rf * size) | _cmp_near(wy, rf * size))
         if refine.any():                                    # subdivide_frusta, :409-467
             sub = rng_[refine]
             subd_x = (sub[:, 2] - sub[:, 0]) >= (sub[:, 3] - sub[:, 1])
@@ -797,15 +830,20 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts):
             t = np.concatenate((t, t[refine]))
             size = np.concatenate((size, size[refine]))
             count = np.concatenate((count, count[refine]))
+            near = np.concatenate((near, near[refine]))
     out_t = np.zeros((int(res_x), int(res_y)), f32)
     out_hit = np.zeros((int(res_x), int(res_y)), np.int32)
     out_count = np.zeros((int(res_x), int(res_y)), np.int32)
-    for r_, tt, hh, cc in fin:                              # subdivide to pixels + write, :469-587
+    out_near = np.zeros((int(res_x), int(res_y)), bool)
+    for r_, tt, hh, cc, nn in fin:                          # subdivide to pixels + write, :469-587
         for i in range(r_.shape[0]):
             x0, y0, x1, y1 = r_[i]
             out_t[x0:x1, y0:y1] = tt[i]
             out_hit[x0:x1, y0:y1] = hh[i]
             out_count[x0:x1, y0:y1] = np.trunc(cc[i]).astype(np.int32)
+            out_near[x0:x1, y0:y1] = nn[i]
+    if trace:
+        return out_t, out_hit, out_count, n_steps, out_near
     return out_t, out_hit, out_count, n_steps
 
 

@@ -138,10 +138,10 @@ def test_cast_rays_frustum(R, name):
     p1 = model_from(g, 'model/relu32x3')
     ps = (p1,) if name == 'one' else (p1, model_from(g, 'model/relu16'))
     fs = tuple(R.generate_implicit(p, 'affine_fixed') for p in ps)
-    t, hid, cnt, _ = R.cast_rays_frustum(fs, ps, cam, opts)
+    t, hid, cnt, _, near = R.cast_rays_frustum(fs, ps, cam, opts, trace=True)
     m = (hid == g[f'frustum/{name}/hit_id']) & (cnt == g[f'frustum/{name}/count']) & \
         np.isclose(t, g[f'frustum/{name}/t'], rtol=1e-5, atol=1e-6)
-    assert m.mean() >= 0.99, m.mean()
+    assert np.all(m | near), np.argwhere(~m & ~near)[:10]
     assert (g[f'frustum/{name}/hit_id'] > 0).sum() > 0
 
 
