@@ -67,7 +67,9 @@ typedef struct niq_model niq_model;
  * AUTO picks the tensor cores where the noise rows x layer width are dense (hidden
  * widths >= 128 and >= 64 rows), FP32 forces FP32 FMA, 3XTF32 forces the tensor cores
  * (split-precision tf32 products; needs every hidden layer activated, widths <= 256 and
- * at most 256 noise rows).  The other modes always use FP32 FMA. */
+ * at most 256 noise rows).  3XTF32 also puts the level-set tree in affine_fixed with
+ * outward rounding on the tensor cores (niq_tree_engine); the other modes and queries
+ * use FP32 FMA. */
 #define NIQ_PRODUCTS_AUTO    0
 #define NIQ_PRODUCTS_FP32    1
 #define NIQ_PRODUCTS_3XTF32  2
@@ -305,7 +307,8 @@ int niq_levelset_tree_growing(const niq_model* model, const niq_bound_opts* opts
                               void* workspace, size_t workspace_bytes, void* stream);
 /* Which engine the level-set tree entry points use for a model and options:
  * NIQ_TREE_ENGINE_TENSOR -- hidden layers' products on the tensor cores (3xTF32, affine_fixed
- *   with outward rounding, products AUTO or 3XTF32, hidden widths <= 64, a scalar output);
+ *   with outward rounding, products 3XTF32, hidden widths <= 64, a scalar output; slower
+ *   than the FP32 engine on the models measured, with wider bounds, so not the default);
  * NIQ_TREE_ENGINE_FP32 -- the FP32 tile engine (the other fixed-mode cases);
  * NIQ_TREE_ENGINE_GROWING -- the growing-term modes, through niq_levelset_tree_growing.
  * Pure host code; the reference has one engine (XLA), so no counterpart. */

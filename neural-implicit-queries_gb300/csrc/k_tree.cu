@@ -215,10 +215,14 @@ __global__ void k_tree_finish(TreeWs* ws, long long* counts) {
     counts[3] = (long long)ws->n_boxes;
 }
 
-// The tensor-core tree serves affine_fixed with outward rounding unless FP32 products
-// are asked for, on the models it supports.
+// The tensor-core tree serves affine_fixed with outward rounding when 3xTF32 products
+// are asked for, on the models it supports.  It is not the default: measured on the
+// 12-sphere model it is slower than the FP32 tile engine (one 8-warp CTA per SM leaves
+// its CUDA-core work -- the err row, the linearisations -- latency-bound), and the
+// larger rounding bound of split products keeps about 1/4 more leaves unknown at 24
+// bisections.
 static bool use_tree_tc(const NiqSpecHeader& H, const niq_bound_opts* opts) {
-    return opts->mode == NIQ_MODE_AFFINE_FIXED && opts->conservative != 0 && opts->products != NIQ_PRODUCTS_FP32 &&
+    return opts->mode == NIQ_MODE_AFFINE_FIXED && opts->conservative != 0 && opts->products == NIQ_PRODUCTS_3XTF32 &&
            tree_tc_eligible(H);
 }
 

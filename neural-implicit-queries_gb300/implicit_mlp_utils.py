@@ -12,8 +12,8 @@ def generate_implicit_from_params(params, mode, **kwargs):
     Extra keywords: ``conservative`` (default True) selects outward rounding;
     ``products`` ('auto', 'fp32', '3xtf32') how dense products are formed where there is a
     choice: the affine_truncate/affine_all engine, and the affine_fixed level-set tree
-    (tensor cores by default on models of hidden width <= 64; 'fp32' keeps the FP32 tile
-    engine)."""
+    ('3xtf32' puts its hidden layers on the tensor cores on models of hidden width <= 64;
+    by default it runs on the FP32 tile engine, which is faster there)."""
     cons = kwargs.get('conservative', True)
     prod = kwargs.get('products', 'auto')
     if mode == 'sdf':

@@ -32,7 +32,7 @@ def tune(niq):
     at.set_params(**old)
 
 
-@pytest.mark.parametrize('products', ['fp32', 'auto'])
+@pytest.mark.parametrize('products', ['fp32', '3xtf32'])
 def test_grid_barrier_gives_up_and_recovers(niq, gpu_ready, tune, products):
     """The persistent tree's level barrier (FP32 tile engine and tensor-core form)."""
     params = niq.workloads.spheres_sdf_model()
@@ -50,7 +50,7 @@ def test_tensor_core_tree_mbarrier_gives_up_and_recovers(niq, gpu_ready, tune):
     """The tensor-core tree's wait on its MMAs: the kernel gives up, still waits for the
     MMAs in flight with the built-in limit, releases tensor memory and returns."""
     params = niq.workloads.spheres_sdf_model()
-    f = gf(niq, params)
+    f = gf(niq, params, products='3xtf32')
     ref = tree_sets(niq, f, params)
     tune.set_params(mbar_polls=1)
     with pytest.raises(niq._lib.NIQError) as e:

@@ -1,10 +1,10 @@
-"""The level-set tree with tensor-core products (csrc/k_tree_tc.cu): the default for
-affine_fixed with outward rounding on models whose hidden layers are at most 64 wide.
+"""The level-set tree with tensor-core products (csrc/k_tree_tc.cu, products='3xtf32';
+affine_fixed with outward rounding on models whose hidden layers are at most 64 wide).
 
 Its bounds are conservative like the FP32 engine's, with a larger rounding term (3xTF32
-products), so against the reference's arithmetic it may only keep MORE boxes unknown;
-interior and exterior nodes must hold the right sign at every FP64 sample; and it gives
-the same node sets in all three schedules (test_gpu_queries.test_tree_schedules_agree)."""
+products), so it keeps somewhat more boxes unknown and against the reference's
+arithmetic it may only keep MORE; interior and exterior nodes must hold the right sign
+at every FP64 sample; and it gives the same node sets in all three schedules."""
 import ctypes as C
 
 import numpy as np
@@ -15,7 +15,7 @@ from parity import box_set_diff
 pytestmark = pytest.mark.gpu
 
 
-def gf(niq, params, products='auto', conservative=True, mode='affine_fixed'):
+def gf(niq, params, products='3xtf32', conservative=True, mode='affine_fixed'):
     return niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=conservative,
                                                                 products=products)[0]
 
@@ -53,6 +53,7 @@ def test_tc_tree_conservative(niq, R, gpu_ready, name):
     params = models(niq)[name]
     assert engine(niq, params, gf(niq, params)) == 1
     assert engine(niq, params, gf(niq, params, 'fp32')) == 0
+    assert engine(niq, params, gf(niq, params, 'auto')) == 0
     lo3, hi3 = -np.ones(3, np.float32), np.ones(3, np.float32)
     depth = 15
     d = niq.kd_tree.construct_uniform_unknown_levelset_tree(gf(niq, params), params, lo3, hi3, split_depth=depth,
@@ -62,12 +63,14 @@ def test_tc_tree_conservative(niq, R, gpu_ready, name):
                                                               with_exterior_nodes=True)
     n = len(d['unknown_node_lower'])
     assert n > 0
-    # against the FP32 engine: the rounding terms differ by about 1e-5 relative, so only
-    # boxes that close to the threshold can change their fate
+    # against the FP32 engine: the split products' rounding bound (about 3.5e-5 relative
+    # at 64 terms against 3.9e-6) keeps more boxes near the surface unknown, and almost
+    # never fewer
     extra, missing = box_set_diff(d['unknown_node_lower'], d['unknown_node_upper'], d32['unknown_node_lower'],
                                   d32['unknown_node_upper'])
     print(f'{name}: {n} leaves; against the FP32 engine {len(extra)} extra, {len(missing)} missing')
-    assert len(extra) + len(missing) <= 0.002 * n + 2
+    assert len(missing) <= 0.002 * n + 2
+    assert len(extra) <= 0.05 * n + 2
     # against the reference's arithmetic (oracle, no outward rounding): conservative bounds
     # are never narrower, so no leaf of the reference goes missing
     if name in ('spheres', 'relu32x3'):
@@ -101,4 +104,4 @@ def test_tc_tree_offset_and_threshold(niq, gpu_ready):
     assert n >= 4096
     extra, missing = box_set_diff(a['unknown_node_lower'], a['unknown_node_upper'], b['unknown_node_lower'],
                                   b['unknown_node_upper'])
-    assert len(extra) + len(missing) <= 0.002 * n + 2
+    assert len(missing) <= 0.002 * n + 2 and len(extra) <= 0.05 * n + 2
