@@ -5,8 +5,9 @@
 // M dimension of a GEMM  D[rows x out] = X[rows x in] * A[in x out]  with up to 256 rows
 // (two M = 128 tiles), computed by tcgen05.mma kind::tf32 as three split-precision
 // products  Xhi*Ahi + Xhi*Alo + Xlo*Ahi  accumulated in fp32 in tensor memory (TMEM,
-// 512 columns: tile t at columns 256 t).  X and the split weights are streamed through a
-// three-stage shared-memory ring in K chunks of 16 (cp.async, two chunks ahead), the MMAs issued by one
+// 512 columns: tile t at columns 256 t).  X (split on the way in) and the split weights are
+// streamed through a three-stage shared-memory ring in K chunks of 16 (weights by
+// cp.async, two chunks ahead), the MMAs issued by one
 // thread and tracked with an mbarrier per stage.  The base and err rows (one vector
 // each) are computed on the CUDA cores.
 //
@@ -15,8 +16,9 @@
 //   2. the linearisation per column (alpha, beta, delta), exactly as the FP32 engine,
 //   3. row magnitudes sum_j alpha_j |D_rj| and the new rows' delta_j,
 //   4. the stable descending rank of every candidate row (src/affine.py:144-162),
-//   5. kept rows, scaled by alpha, written split (hi, lo) to the CTA's scratch as the next
-//      layer's X, in rank order; dropped rows folded into err.
+//   5. kept rows, scaled by alpha, written in fp32 to the CTA's scratch as the next
+//      layer's X, in rank order (split into hi and lo as each K chunk is staged); dropped
+//      rows folded into err.
 // The first layer (3 inputs) and the last (1 output) are computed on the CUDA cores.
 // TMEM lanes past the box's rows and columns past the layer's width hold stale values;
 // every epilogue read masks them.
@@ -41,7 +43,7 @@ constexpr int kTcRows = 256;                   // noise rows one GEMM holds
 constexpr int kTcTrLD = 17;                    // transpose buffer row stride (16 columns)
 constexpr int kTcStages = 3;                   // shared-memory pipeline depth
 constexpr int kTcStage = 4 * kTcRows * kTcKC;  // floats: X hi, X lo, W hi, W lo
-constexpr int kTcXFloats = kTcRows * NIQ_MAX_WIDTH;  // one split half of a CTA's X scratch
+constexpr int kTcXFloats = kTcRows * NIQ_MAX_WIDTH;  // a CTA's X scratch (fp32, split while staging)
 
 // dynamic shared memory (floats)
 constexpr int kTcOffTr = kTcStages * kTcStage;
@@ -64,7 +66,7 @@ struct TcArgs {
     float offset;
     int* sign_out;
     float* lohi_out;
-    float* xs;                         // per CTA: 2 * kTcXFloats (hi, lo)
+    float* xs;                         // per CTA: kTcXFloats (the next layer's X in fp32)
     int* status;
     long long mbar_polls;              // poll limit of the waits on the MMAs
 };
@@ -170,8 +172,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     // bit s of `pending` marks it, bit s of `phase` is the parity of its next completion.
     // Register bit masks, not arrays indexed by the stage, which would live in local memory.
     uint32_t pending = 0u, phase = 0u;
-    float* xs_hi = a.xs + (size_t)blockIdx.x * 2 * kTcXFloats;
-    float* xs_lo = xs_hi + kTcXFloats;
+    float* xs = a.xs + (size_t)blockIdx.x * kTcXFloats;
     const int tile = warp >> 2;
     const int row = tile * 128 + (warp & 3) * 32 + lane;  // this thread's noise row
     const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(tile * 256);
@@ -276,13 +277,18 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                         const int s = c % kTcStages;
                         float* stg = smem + s * kTcStage;
                         const int xf4 = mt * 128 * kTcKC / 4, wf4 = o16 * kTcKC / 4;
-                        const float* xsrc_h = xs_hi + c * kTcRows * kTcKC;
-                        const float* xsrc_l = xs_lo + c * kTcRows * kTcKC;
+                        const float* xsrc = xs + c * kTcRows * kTcKC;
                         const float* wsrc_h = whi + (long long)c * o16 * kTcKC;
                         const float* wsrc_l = wlo + (long long)c * o16 * kTcKC;
+                        // X is kept once in fp32 and split here: half the scratch traffic of
+                        // keeping hi and lo (the split weights stream with cp.async)
                         for (int i = tid; i < xf4; i += kTcNT) {
-                            cp_async16(stg + 4 * i, xsrc_h + 4 * i);
-                            cp_async16(stg + kTcRows * kTcKC + 4 * i, xsrc_l + 4 * i);
+                            const float4 v = __ldcg(reinterpret_cast<const float4*>(xsrc) + i);
+                            const float4 h = make_float4(tc::tf32_hi(v.x), tc::tf32_hi(v.y), tc::tf32_hi(v.z),
+                                                         tc::tf32_hi(v.w));
+                            *reinterpret_cast<float4*>(stg + 4 * i) = h;
+                            *reinterpret_cast<float4*>(stg + kTcRows * kTcKC + 4 * i) =
+                                make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
                         }
                         for (int i = tid; i < wf4; i += kTcNT) {
                             cp_async16(stg + 2 * kTcRows * kTcKC + 4 * i, wsrc_h + 4 * i);
@@ -448,14 +454,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     for (int q = 0; q < 8; ++q) {
                         const int k = ch * 32 + 4 * q;
                         if (k >= o16) break;
-                        float4 h, l;
-                        h.x = tc::tf32_hi(val[4 * q]);     l.x = val[4 * q] - h.x;
-                        h.y = tc::tf32_hi(val[4 * q + 1]); l.y = val[4 * q + 1] - h.y;
-                        h.z = tc::tf32_hi(val[4 * q + 2]); l.z = val[4 * q + 2] - h.z;
-                        h.w = tc::tf32_hi(val[4 * q + 3]); l.w = val[4 * q + 3] - h.w;
-                        const int xi = x_index(my_rank, k);
-                        *reinterpret_cast<float4*>(xs_hi + xi) = h;
-                        *reinterpret_cast<float4*>(xs_lo + xi) = l;
+                        *reinterpret_cast<float4*>(xs + x_index(my_rank, k)) =
+                            make_float4(val[4 * q], val[4 * q + 1], val[4 * q + 2], val[4 * q + 3]);
                     }
                 }
 #pragma unroll
@@ -469,16 +469,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             if (j < out) {
                 const int rk = s_rank[nrows + j];
                 if (rk < keep) {
-                    const float dh = tc::tf32_hi(delta), dl = delta - dh;
-                    for (int k = 0; k < o16; k += 4) {
-                        const float4 h = make_float4(j == k ? dh : 0.f, j == k + 1 ? dh : 0.f, j == k + 2 ? dh : 0.f,
-                                                     j == k + 3 ? dh : 0.f);
-                        const float4 l = make_float4(j == k ? dl : 0.f, j == k + 1 ? dl : 0.f, j == k + 2 ? dl : 0.f,
-                                                     j == k + 3 ? dl : 0.f);
-                        const int xi = x_index(rk, k);
-                        *reinterpret_cast<float4*>(xs_hi + xi) = h;
-                        *reinterpret_cast<float4*>(xs_lo + xi) = l;
-                    }
+                    for (int k = 0; k < o16; k += 4)
+                        *reinterpret_cast<float4*>(xs + x_index(rk, k)) =
+                            make_float4(j == k ? delta : 0.f, j == k + 1 ? delta : 0.f, j == k + 2 ? delta : 0.f,
+                                        j == k + 3 ? delta : 0.f);
                 } else {
                     e = add_up<C>(e, delta);
                 }
@@ -520,9 +514,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 float d = 0.f;
                 for (int k = 0; k < L.in; k += 4) {
                     const int xi = x_index(row, k);
-                    const float4 h = *reinterpret_cast<const float4*>(xs_hi + xi);
-                    const float4 l = *reinterpret_cast<const float4*>(xs_lo + xi);
-                    const float x4[4] = {h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w};
+                    const float4 xv = *reinterpret_cast<const float4*>(xs + xi);
+                    const float x4[4] = {xv.x, xv.y, xv.z, xv.w};
                     for (int q = 0; q < 4 && k + q < L.in; ++q) d = fmaf(x4[q], A[(k + q) * L.out_pad], d);
                 }
                 part_s = fabsf(d);
@@ -631,7 +624,7 @@ bool wide_use_tc(const NiqSpecHeader& H, const niq_bound_opts& o, int v) {
 }
 
 size_t wide_tc_workspace_bytes() {
-    return (size_t)device_info().sm_count * 2 * kTcXFloats * 4 + 256 + 256;
+    return (size_t)device_info().sm_count * kTcXFloats * 4 + 256 + 256;
 }
 
 int wide_tc_classify(const niq_model* m, const niq_bound_opts& o, long long n, const float* center, const float* vecs,
