@@ -408,9 +408,32 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                                           : make_float4(0.f, 0.f, 0.f, 0.f);
                         a[4 * q + 0] = av.x; a[4 * q + 1] = av.y; a[4 * q + 2] = av.z; a[4 * q + 3] = av.w;
                     }
-                    if constexpr (NABS > 0) {
-                        // bound rows: issue-bound, so packed FMAs pay for the pair rebuilt
-                        // from each input value
+                    if constexpr (NABS == 1) {
+                        // affine tiles: the signed rows with packed FMAs (issue-bound, so
+                        // they pay for the pair rebuilt from each input value); the one
+                        // |A| row with scalar FMAs, whose |.| is an operand modifier, where
+                        // a packed form would need the absolute weights built first.  Each
+                        // lane of a packed FMA is a correctly rounded fp32 FMA, so the
+                        // results are those of scalar FMAs either way.
+                        float2 w[COLS / 2];
+#pragma unroll
+                        for (int c = 0; c < COLS / 2; ++c) w[c] = make_float2(a[2 * c], a[2 * c + 1]);
+#pragma unroll
+                        for (int r = 0; r < R - 1; ++r) {
+                            const float xv = kk == 0 ? x[r].x : kk == 1 ? x[r].y : kk == 2 ? x[r].z : x[r].w;
+                            const float2 x2 = make_float2(xv, xv);
+#pragma unroll
+                            for (int c = 0; c < COLS / 2; ++c) acc.pair(r, c) = __ffma2_rn(x2, w[c], acc.pair(r, c));
+                        }
+                        {
+                            const float xv = kk == 0 ? x[R - 1].x : kk == 1 ? x[R - 1].y : kk == 2 ? x[R - 1].z
+                                                                                              : x[R - 1].w;
+#pragma unroll
+                            for (int c = 0; c < COLS; ++c) ACC(R - 1, c) = fmaf(xv, fabsf(a[c]), ACC(R - 1, c));
+                        }
+                    } else if constexpr (NABS > 0) {
+                        // slope tiles (four |A| rows): packed FMAs, the absolute weights
+                        // built once per input and shared by those rows
                         float2 w[COLS / 2], wa[COLS / 2];
 #pragma unroll
                         for (int c = 0; c < COLS / 2; ++c) {
