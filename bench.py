@@ -299,6 +299,8 @@ def run_ours(args):
 # divided by its boxes): the level arrays stay in L2, so a box costs well under its 24 B
 # of node I/O.  Keyed by the engine code of niq_tree_engine.
 TREE_DRAM_BYTES_PER_BOX = {0: (148480 + 6912) / 332953}
+TREE_DRAM_SOURCE = {0: "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the 18-bisection tree "
+                       "(155.4 KB for 332,953 boxes), scaled by boxes"}
 
 
 def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
@@ -316,8 +318,7 @@ def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
            else "k_tree (persistent level-set tree)",
            "achieved": achieved, "unit": "TFLOP/s", "flops_per_box": bf,
            "traffic": per_box * n_boxes if per_box is not None else None,
-           "traffic_source": "ncu dram bytes per box of the same kernel on the 24-bisection tree" if per_box
-           else "not captured for this kernel"}
+           "traffic_source": TREE_DRAM_SOURCE.get(engine, "not captured for this kernel")}
     if engine == 1:
         tensor = n_boxes * 3 * 2 * 4 * hidden / t_tree / 1e12
         out.update({"bound": "tensor", "peak": tf32_peak, "frac": achieved / tf32_peak,
