@@ -438,11 +438,12 @@ def precision_sample(niq, steps, warmup):
             ts.append(e0.elapsed_time(e1) / 1e3)
         return r, sum(ts) / len(ts)
     out = {}
+    dm = niq.mlp.device_model(params)   # the resident model: no per-call hashing of its weights
     for name, products in (("3xtf32", "3xtf32"), ("fp32", "fp32")):
         f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_truncate', conservative=True,
                                                                     products=products, affine_n_truncate=256)
-        _, tb = timed(lambda: f.bounds_general_box(params, c, vv), max(1, steps // 4), 1)
-        r, tr = timed(lambda: niq.queries.cast_rays((f,), (params,), rs, ds, opts, return_device=True), 1, 1)
+        _, tb = timed(lambda: f.bounds_general_box(dm, c, vv), max(1, steps // 4), 1)
+        r, tr = timed(lambda: niq.queries.cast_rays((f,), (dm,), rs, ds, opts, return_device=True), 1, 1)
         out[name] = {"boxes_per_s": nb / tb, "classify_ms": tb * 1e3, "rays_per_s": rs.shape[0] / tr,
                      "cast_ms": tr * 1e3, "ray_steps": int(r[2].sum().item()),
                      "achieved_tflops": nb * fl / tb / 1e12}
@@ -663,15 +664,16 @@ def run_precision(args):
                                         "boxes": nb, "conservative": True}}
     if args.quick:   # profiling runs: the tensor-core classification only
         forms = forms[2:]
+    dm = niq.mlp.device_model(params)   # the resident model: no per-call hashing of its weights
     for name, mode, kw, products, fl in forms:
         f, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=True,
                                                                     products=products, **kw)
         if args.quick:
-            _, tb = timed(lambda: f.bounds_general_box(params, c, vv), 1, 1)
+            _, tb = timed(lambda: f.bounds_general_box(dm, c, vv), 1, 1)
             print(json.dumps({"quick": True, "classify_ms": tb * 1e3, "boxes": nb}))
             return
-        r, t = timed(lambda: niq.queries.cast_rays((f,), (params,), rs, ds, opts, return_device=True), 1, 1)
-        _, tb = timed(lambda: f.bounds_general_box(params, c, vv), 3, 1)
+        r, t = timed(lambda: niq.queries.cast_rays((f,), (dm,), rs, ds, opts, return_device=True), 1, 1)
+        _, tb = timed(lambda: f.bounds_general_box(dm, c, vv), 3, 1)
         tf = nb * fl / tb / 1e12
         row = {"rays_per_s": rs.shape[0] / t, "cast_ms": t * 1e3, "ray_steps": int(r[2].sum().item()),
                "hits": int((r[1] > 0).sum().item()), "boxes_per_s": nb / tb, "classify_ms": tb * 1e3,

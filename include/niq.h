@@ -134,6 +134,12 @@ int niq_model_info(const niq_model* model, int32_t* max_width, int32_t* n_layers
  *      src/mlp.py:253-347) --------------------------------------------------------- */
 int niq_eval_points(const niq_model* model, int64_t n, const float* xyz, float* out,
                     void* stream);
+/* Value (val_out (n), may be NULL) and gradient (grad_out (n,3)) of the MLP at n points:
+ * the derivative jax.jacfwd takes of the point function for outward_normal(...,
+ * method='autodiff') (src/render.py:61-63), by forward-mode tangents with JAX's
+ * activation derivatives (relu' = 0 at x <= 0, elu' = exp(x) at x <= 0). */
+int niq_eval_gradients(const niq_model* model, int64_t n, const float* xyz, float* val_out,
+                       float* grad_out, void* stream);
 
 /* ---- range bounds: classify_general_box (src/affine.py:34-55,
  *      src/slope_interval.py:29-51).  center (n,3), vecs (n,v,3) with 1 <= v <= 3.
@@ -224,6 +230,13 @@ size_t niq_outward_normals_workspace_size(int64_t n);
 int niq_outward_normals(const niq_model* const* models, int32_t nfunc, int64_t n, const float* hit_pos,
                         const int32_t* hit_id, float eps, float* normals_out, void* workspace,
                         size_t workspace_bytes, void* stream);
+/* outward_normals(..., method='autodiff') (src/render.py:61-63,81-90): the normalised
+ * gradient (niq_eval_gradients) of the function each point hit, zeros where none; a
+ * workspace of niq_outward_normals_autodiff_workspace_size(n) bytes. */
+size_t niq_outward_normals_autodiff_workspace_size(int64_t n);
+int niq_outward_normals_autodiff(const niq_model* const* models, int32_t nfunc, int64_t n,
+                                 const float* hit_pos, const int32_t* hit_id, float* normals_out,
+                                 void* workspace, size_t workspace_bytes, void* stream);
 /* Shading into a device RGB buffer (n, 3): shading 0 = 'normal', 1 = 'matcap_color' with
  * matcaps a device array (4, matcap_h, matcap_w, 3) of the r, g, b, k images and colors
  * a host array (ncolors, 3), one per function.  up_dir is host (3).  Pixels without a
@@ -231,6 +244,12 @@ int niq_outward_normals(const niq_model* const* models, int32_t nfunc, int64_t n
 int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
                     const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
                     const float* colors, int32_t ncolors, int32_t tonemap, float* rgb_out, void* stream);
+/* 'matcap_color' shading with a color per pixel: pixel_colors a device array (n, 3), the
+ * values of the reference's shading_color_func at the hit positions
+ * (src/render.py:193-206), in place of the per-function colors. */
+int niq_shade_image_pixel_colors(int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
+                                 const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
+                                 const float* pixel_colors, int32_t tonemap, float* rgb_out, void* stream);
 
 /* ---- level-set kd-tree: construct_uniform_unknown_levelset_tree
  *      (src/kd_tree.py:19-218) ------------------------------------------------------ *

@@ -32,6 +32,14 @@ def to_dev(x, dtype='float32'):
     return t.from_numpy(a).to('cuda', non_blocking=False), 'numpy'
 
 
+def to_numpy(x):
+    """A NumPy array of an array-like or a (CPU or CUDA) tensor."""
+    t = torch()
+    if isinstance(x, t.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
 def back(t, kind):
     if kind == 'cuda':
         return t

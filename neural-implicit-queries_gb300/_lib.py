@@ -85,6 +85,7 @@ _SIGS = {
     'niq_model_destroy': (C.c_int, [_P]),
     'niq_model_info': (C.c_int, [_P, C.POINTER(_I32), C.POINTER(_I32)]),
     'niq_eval_points': (C.c_int, [_P, _I64, _P, _P, _P]),
+    'niq_eval_gradients': (C.c_int, [_P, _I64, _P, _P, _P, _P]),
     'niq_classify_workspace_size': (_SZ, [_P, C.POINTER(BoundOpts), _I64, _I32]),
     'niq_classify_boxes': (C.c_int, [_P, C.POINTER(BoundOpts), _I64, _P, _P, _I32, _F32, _P, _P, _P, _SZ, _P]),
     'niq_cast_rays_workspace_size': (_SZ, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I64]),
@@ -104,7 +105,10 @@ _SIGS = {
                                       _SZ, _P]),
     'niq_outward_normals_workspace_size': (_SZ, [_I64]),
     'niq_outward_normals': (C.c_int, [C.POINTER(_P), _I32, _I64, _P, _P, _F32, _P, _P, _SZ, _P]),
+    'niq_outward_normals_autodiff_workspace_size': (_SZ, [_I64]),
+    'niq_outward_normals_autodiff': (C.c_int, [C.POINTER(_P), _I32, _I64, _P, _P, _P, _P, _SZ, _P]),
     'niq_shade_image': (C.c_int, [_I32, _I64, _P, _P, _P, _PF, _P, _I32, _I32, _PF, _I32, _I32, _P, _P]),
+    'niq_shade_image_pixel_colors': (C.c_int, [_I64, _P, _P, _P, _PF, _P, _I32, _I32, _P, _I32, _P, _P]),
     'niq_levelset_tree_plain': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P,
                                           _SZ, _P]),
     'niq_levelset_tree_batches': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _I64,

@@ -1,6 +1,7 @@
 // k_eval.cu -- point evaluation and box classification over caller-given batches.
 //
 // niq_eval_points      : ImplicitFunction.__call__ (src/affine.py:26-28) for N points.
+// niq_eval_gradients   : value and gradient at N points (jax.jacfwd, src/render.py:61-63).
 // niq_classify_boxes   : classify_general_box (src/affine.py:34-55,
 //                        src/slope_interval.py:29-51) for N general boxes.
 // Both are persistent grid-stride kernels over CTA tiles of the fused tile engine.
@@ -40,6 +41,49 @@ __global__ void __launch_bounds__(kNT) k_eval_points(NiqModelRef M, long long n,
         for (int r = g; r < 8; r += TPI) {
             const long long p = tile * per_tile + item * 8 + r;
             if (p < n) out[p] = o[item * 8 + r];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- gradients
+// Forward-mode derivatives: an item holds two points, each a value row and the three
+// tangent rows d/dx, d/dy, d/dz (input: the point and the unit vectors), which the dense
+// rule multiplies by A and the activation by its derivative at the pre-activation.
+template <int TPI>
+__global__ void __launch_bounds__(kNT) k_eval_grad(NiqModelRef M, long long n, const float* __restrict__ xyz,
+                                                   float* __restrict__ val, float* __restrict__ grad,
+                                                   int fixed_floats, int sw_cap, int resident) {
+    using Cfg = TileCfg<8, 0, TPI, kNT>;
+    extern __shared__ float4 smem4[];
+    float* smem = reinterpret_cast<float*>(smem4);
+    float* st = smem;
+    float* o = st + Cfg::STATE_FLOATS;
+    float* sW = smem + fixed_floats;
+    __shared__ NiqSpecHeader H;
+    load_header(H, M.hdr);
+    __syncthreads();
+    if (resident) stage_floats(sW, M.w, H.n_weight_floats);
+    const RowPlan plan{ROWS_JVP, 0, 0};
+    const int item = threadIdx.x / TPI, g = threadIdx.x % TPI;
+    const long long per_tile = (long long)Cfg::ITEMS * 2;
+    for (long long tile = blockIdx.x; tile * per_tile < n; tile += gridDim.x) {
+        float* xs = st + item * Cfg::R * Cfg::LD;
+        for (int r = g; r < 8; r += TPI) {
+            const long long p = tile * per_tile + item * 2 + r / 4;
+            const int kind = r % 4;   // 0: the point, 1..3: the tangent of input kind - 1
+            float4 v = make_float4(kind == 1 ? 1.f : 0.f, kind == 2 ? 1.f : 0.f, kind == 3 ? 1.f : 0.f, 0.f);
+            if (kind == 0 && p < n) { v.x = xyz[3 * p]; v.y = xyz[3 * p + 1]; v.z = xyz[3 * p + 2]; }
+            *reinterpret_cast<float4*>(xs + r * Cfg::LD) = v;
+        }
+        __syncthreads();
+        tile_forward<Cfg, false>(H, M.w, sW, sw_cap, resident, plan, st, o);
+        for (int r = g; r < 8; r += TPI) {
+            const long long p = tile * per_tile + item * 2 + r / 4;
+            const int kind = r % 4;
+            if (p >= n) continue;
+            if (kind == 0) { if (val) val[p] = o[item * 8 + r]; }
+            else grad[3 * p + kind - 1] = o[item * 8 + r];
         }
         __syncthreads();
     }
@@ -152,6 +196,27 @@ int niq_eval_points(const niq_model* model, int64_t n, const float* xyz, float* 
         rc = launch_tile_kernel(kern, 8, TPI, model, tiles, s, p, grid);
         if (rc) return rc;
         kern<<<grid, kNT, p.bytes, s>>>(model->ref(), n, xyz, out, p.fixed_floats, p.sw_cap, p.resident);
+    });
+    NIQ_CUDA(cudaGetLastError());
+    return rc;
+}
+
+int niq_eval_gradients(const niq_model* model, int64_t n, const float* xyz, float* val_out, float* grad_out,
+                       void* stream) {
+    NIQ_REQUIRE(model && (n == 0 || (xyz && grad_out)), NIQ_ERR_INVALID_ARG, "null argument");
+    NIQ_REQUIRE(n >= 0, NIQ_ERR_INVALID_ARG, "negative count");
+    if (n == 0) return NIQ_OK;
+    const int tpi = tpi_for_width(model->hdr.max_width);
+    cudaStream_t s = as_stream(stream);
+    int rc = NIQ_OK;
+    NIQ_DISPATCH_TPI(tpi, {
+        auto kern = k_eval_grad<TPI>;
+        SmemPlan p;
+        int grid = 0;
+        const long long tiles = (n + (kNT / TPI) * 2 - 1) / ((kNT / TPI) * 2);
+        rc = launch_tile_kernel(kern, 8, TPI, model, tiles, s, p, grid);
+        if (rc) return rc;
+        kern<<<grid, kNT, p.bytes, s>>>(model->ref(), n, xyz, val_out, grad_out, p.fixed_floats, p.sw_cap, p.resident);
     });
     NIQ_CUDA(cudaGetLastError());
     return rc;

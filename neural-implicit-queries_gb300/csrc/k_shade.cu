@@ -41,6 +41,19 @@ __global__ void k_normal_combine(long long n, int f, const float* __restrict__ v
     }
 }
 
+// Normals from gradients (method 'autodiff'): where the point hit function f + 1, its
+// normalised gradient (geometry.normalize, src/geometry.py:12-13).
+__global__ void k_grad_combine(long long n, int f, const float* __restrict__ grad, const int* __restrict__ hit_id,
+                               float* __restrict__ normals) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        if (f == 0) normals[3 * p] = normals[3 * p + 1] = normals[3 * p + 2] = 0.f;
+        if (hit_id[p] != f + 1) continue;
+        const float* g = grad + 3 * p;
+        const float nrm = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g[0], g[0]), __fmul_rn(g[1], g[1])), __fmul_rn(g[2], g[2])));
+        for (int k = 0; k < 3; ++k) normals[3 * p + k] = __fdiv_rn(g[k], nrm);
+    }
+}
+
 struct ShadeArgs {
     int shading;          // 0 normal, 1 matcap_color
     float up[3];          // up direction as the caller gives it
@@ -49,6 +62,7 @@ struct ShadeArgs {
     float colors[8][3];   // per function (1-based hit id)
     int ncolors;
     int tonemap;
+    const float* pix;     // per-pixel colors (n, 3) of shading_color_func, or null
 };
 
 // one channel of a matcap at (x, y): bilinear, indices clamped to the image (src/render.py:184-187)
@@ -98,7 +112,9 @@ __global__ void k_shade(long long n, ShadeArgs a, const float* __restrict__ dirs
             const float y = __fmul_rn(__fdiv_rn(__fadd_rn(-mv, 1.f), 2.f), (float)a.mw);
             const int h = hit_id[p];
             float col[3] = {1.f, 1.f, 1.f};
-            if (h >= 1 && h <= a.ncolors)
+            if (a.pix)
+                for (int k = 0; k < 3; ++k) col[k] = a.pix[3 * p + k];
+            else if (h >= 1 && h <= a.ncolors)
                 for (int k = 0; k < 3; ++k) col[k] = a.colors[h - 1][k];
             const float ck = __fsub_rn(1.f, __fadd_rn(__fadd_rn(col[0], col[2]), col[1]));
             const long long plane = (long long)a.mh * a.mw * 3;
@@ -169,9 +185,34 @@ int niq_outward_normals(const niq_model* const* models, int32_t nfunc, int64_t n
     return NIQ_OK;
 }
 
-int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
-                    const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
-                    const float* colors, int32_t ncolors, int32_t tonemap, float* rgb_out, void* stream) {
+size_t niq_outward_normals_autodiff_workspace_size(int64_t n) {
+    return (size_t)(n > 0 ? n : 0) * 3 * 4 + 512;
+}
+
+int niq_outward_normals_autodiff(const niq_model* const* models, int32_t nfunc, int64_t n, const float* hit_pos,
+                                 const int32_t* hit_id, float* normals_out, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
+    NIQ_REQUIRE(models && nfunc >= 1 && nfunc <= 8, NIQ_ERR_INVALID_ARG, "nfunc must be in [1, 8]");
+    NIQ_REQUIRE(n >= 0, NIQ_ERR_INVALID_ARG, "n < 0");
+    if (n == 0) return NIQ_OK;
+    NIQ_REQUIRE(hit_pos && hit_id && normals_out, NIQ_ERR_INVALID_ARG, "null array");
+    const size_t need = niq_outward_normals_autodiff_workspace_size(n);
+    NIQ_REQUIRE(workspace && workspace_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", need);
+    cudaStream_t s = as_stream(stream);
+    float* grad = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    for (int f = 0; f < nfunc; ++f) {
+        NIQ_REQUIRE(models[f], NIQ_ERR_INVALID_ARG, "null model %d", f);
+        int rc = niq_eval_gradients(models[f], n, hit_pos, nullptr, grad, stream);
+        if (rc) return rc;
+        k_grad_combine<<<grid_for(n), 256, 0, s>>>(n, f, grad, hit_id, normals_out);
+        NIQ_CUDA(cudaGetLastError());
+    }
+    return NIQ_OK;
+}
+
+static int shade(int32_t shading, int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
+                 const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w, const float* colors,
+                 int32_t ncolors, const float* pixel_colors, int32_t tonemap, float* rgb_out, void* stream) {
     NIQ_REQUIRE(shading == 0 || shading == 1, NIQ_ERR_INVALID_ARG, "shading must be 0 (normal) or 1 (matcap_color)");
     NIQ_REQUIRE(n >= 0, NIQ_ERR_INVALID_ARG, "n < 0");
     if (n == 0) return NIQ_OK;
@@ -183,9 +224,10 @@ int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const flo
     a.mh = matcap_h;
     a.mw = matcap_w;
     a.ncolors = 0;
+    a.pix = pixel_colors;
     if (shading == 1) {
         NIQ_REQUIRE(up_dir && matcaps && matcap_h >= 1 && matcap_w >= 1, NIQ_ERR_INVALID_ARG, "matcap shading needs up_dir and matcaps");
-        NIQ_REQUIRE(colors && ncolors >= 1 && ncolors <= 8, NIQ_ERR_INVALID_ARG, "1 to 8 colors needed");
+        NIQ_REQUIRE(pixel_colors || (colors && ncolors >= 1 && ncolors <= 8), NIQ_ERR_INVALID_ARG, "1 to 8 colors needed");
         // orthogonal_dir(up_dir, ray_dir) removes the ray's component from up_dir as given
         // (src/geometry.py:15-19)
         for (int k = 0; k < 3; ++k) a.up[k] = up_dir[k];
@@ -196,6 +238,21 @@ int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const flo
     k_shade<<<grid_for(n), 256, 0, as_stream(stream)>>>(n, a, ray_dirs, normals, hit_id, rgb_out);
     NIQ_CUDA(cudaGetLastError());
     return NIQ_OK;
+}
+
+int niq_shade_image(int32_t shading, int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
+                    const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
+                    const float* colors, int32_t ncolors, int32_t tonemap, float* rgb_out, void* stream) {
+    return shade(shading, n, ray_dirs, normals, hit_id, up_dir, matcaps, matcap_h, matcap_w, colors, ncolors, nullptr,
+                 tonemap, rgb_out, stream);
+}
+
+int niq_shade_image_pixel_colors(int64_t n, const float* ray_dirs, const float* normals, const int32_t* hit_id,
+                                 const float* up_dir, const float* matcaps, int32_t matcap_h, int32_t matcap_w,
+                                 const float* pixel_colors, int32_t tonemap, float* rgb_out, void* stream) {
+    NIQ_REQUIRE(n == 0 || pixel_colors, NIQ_ERR_INVALID_ARG, "null pixel colors");
+    return shade(1, n, ray_dirs, normals, hit_id, up_dir, matcaps, matcap_h, matcap_w, nullptr, 0, pixel_colors,
+                 tonemap, rgb_out, stream);
 }
 
 }  // extern "C"

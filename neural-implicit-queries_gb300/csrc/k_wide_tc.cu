@@ -46,12 +46,11 @@ constexpr int kTcStage = 4 * kTcRows * kTcKC;  // floats: X hi, X lo, W hi, W lo
 constexpr int kTcXFloats = kTcRows * NIQ_MAX_WIDTH;  // a CTA's X scratch (fp32, split while staging)
 
 // dynamic shared memory (floats)
-constexpr int kTcOffTr = kTcStages * kTcStage;
-constexpr int kTcOffPart = kTcOffTr + kTcRows * kTcTrLD;
-constexpr int kTcOffVec = kTcOffPart + 256;
-constexpr int kTcOffMag = kTcOffVec + 8 * 256;
-constexpr int kTcOffRank = kTcOffMag + 512;
-constexpr int kTcSmemFloats = kTcOffRank + 512;
+constexpr int kTcOffTr = kTcStages * kTcStage;           // per-warp 32 x 17 transpose tiles
+constexpr int kTcOffVec = kTcOffTr + kTcRows * kTcTrLD;     // per-neuron vectors
+constexpr int kTcOffOut = kTcOffVec + 8 * 256;             // output layer's column, scan counts, select digit
+constexpr int kTcOffNew = kTcOffOut + 512;                 // kept new rows: neuron, delta
+constexpr int kTcSmemFloats = kTcOffNew + 512;
 constexpr size_t kTcSmemBytes = (size_t)kTcSmemFloats * 4;
 
 struct TcArgs {
@@ -92,66 +91,142 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 // every committed group but the most recent one complete
 __device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// Stable descending rank of value v at index me among s[0..n):
-//   #{i : s_i > v} + #{i < me : s_i == v}   (the order of a stable descending argsort).
-// Below the calling warp's window [w0, w0 + 32) every index is < me, so the test is
-// s_i >= v; above it every index is > me, so it is s_i > v.  Those two ranges go in
-// float4 steps; only the window compares indices.  s is 16-byte aligned, w0 <= me < n.
-__device__ __forceinline__ int stable_rank(const float* s, int n, float v, int me, int w0) {
-    const int lo = w0 & ~3;
-    int hi = (w0 + 32 + 3) & ~3;
-    if (hi > n) hi = n;
-    int rk = 0;
-    for (int i = 0; i < lo; i += 4) {
-        const float4 q = *reinterpret_cast<const float4*>(s + i);
-        rk += (q.x >= v) + (q.y >= v) + (q.z >= v) + (q.w >= v);
+// Column sums over a warp's 32 rows (lane = row) of 32 values per lane: lane l receives
+// the sum of column l.  The values go through the warp's own 32 x 17 shared-memory tile,
+// 16 columns at a time (conflict-free rows and columns), with warp-level sync only.
+template <bool C>
+__device__ __forceinline__ float warp_column_sum32(const float* val, float* wt, int lane) {
+    float res = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) wt[lane * kTcTrLD + i] = val[16 * h + i];
+        __syncwarp();
+        const int col = lane & 15, r0 = (lane >> 4) * 16;
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) s = add_up<C>(s, wt[(r0 + q) * kTcTrLD + col]);
+        s = add_up<C>(s, __shfl_xor_sync(0xffffffffu, s, 16));
+        if ((lane >> 4) == h) res = s;
+        __syncwarp();
     }
-    for (int i = lo; i < hi; ++i) rk += (s[i] > v) || (s[i] == v && i < me);
-    const int n4 = n & ~3;
-    int i = hi;
-    for (; i < n4; i += 4) {
-        const float4 q = *reinterpret_cast<const float4*>(s + i);
-        rk += (q.x > v) + (q.y > v) + (q.z > v) + (q.w > v);
-    }
-    for (i = (i > hi ? i : hi); i < n; ++i) rk += s[i] > v;
-    return rk;
+    return res;
 }
 
-// Column sums over the CTA's rows of one 16-column group: every thread contributes
-// val[i] for its row; thread t < 16 receives the sum of column t.
-template <bool C>
-__device__ __forceinline__ float column_sum16(const float* val, int row, float* tr, float* part) {
-    const int tid = threadIdx.x;
+// Radix-select step for one lane of the searching warp.  The lane owns the 8 digits
+// 255 - 8 lane - e (e = 0..7, descending) of the 256-bin histogram h; `above` keys have a
+// larger digit.  If the kk-th largest key has one of the lane's digits, the lane writes
+// that digit to sel[0] and the number of keys with a larger digit to sel[1].
+__device__ __forceinline__ void kth_digit_in_lane(const int* h, int lane, int above, int kk, int* sel) {
+    for (int e = 0; e < 8; ++e) {
+        const int d = 255 - 8 * lane - e;
+        if (above < kk && kk <= above + h[d]) {
+            sel[0] = d;
+            sel[1] = above;
+            return;
+        }
+        above += h[d];
+    }
+}
+
+// The K-th largest (1 <= K <= number of valid keys) of the block's keys, two per thread
+// (k0 if v0, k1 if v1): nonnegative floats as bit patterns, whose unsigned order is their
+// order (a NaN counts as the largest).  Four passes over 8-bit digits, most significant
+// first.  A pass histograms the digit of the keys that match the digits found so far
+// (lanes with the same digit add once), then one warp finds the digit that holds the
+// K-th largest: each lane owns 8 digits in descending order and a shuffle scan gives the
+// number of keys above them.  Two histogram buffers alternate, so clearing the next one
+// overlaps the search.  Returns the key; *n_gt receives the number of keys above it.
+__device__ uint32_t block_kth_largest(uint32_t k0, bool v0, uint32_t k1, bool v1, int K, int* hist, int* sel,
+                                      int* n_gt) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    hist[tid] = 0;   // buffer 0 (kTcNT == 256 bins)
+    __syncthreads();
+    uint32_t prefix = 0u, mask = 0u;
+    int kk = K;
+#pragma unroll 1
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 24 - 8 * pass;
+        int* h = hist + 256 * (pass & 1);
+        const bool m0 = v0 && (k0 & mask) == prefix, m1 = v1 && (k1 & mask) == prefix;
+        {
+            const uint32_t d = m0 ? (k0 >> shift) & 255u : 256u + (uint32_t)lane;   // unmatched: a group of one
+            const uint32_t grp = __match_any_sync(0xffffffffu, d);
+            if (m0 && lane == __ffs(grp) - 1) atomicAdd(&h[d], __popc(grp));
+        }
+        {
+            const uint32_t d = m1 ? (k1 >> shift) & 255u : 256u + (uint32_t)lane;
+            const uint32_t grp = __match_any_sync(0xffffffffu, d);
+            if (m1 && lane == __ffs(grp) - 1) atomicAdd(&h[d], __popc(grp));
+        }
+        __syncthreads();
+        if (tid < 32) {
+            int tot = 0;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) tr[row * kTcTrLD + i] = val[i];
+            for (int e = 0; e < 8; ++e) tot += h[255 - 8 * lane - e];
+            int incl = tot;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
+            }
+            kth_digit_in_lane(h, lane, incl - tot, kk, sel);
+        } else {
+            int* hn = hist + 256 * ((pass + 1) & 1);
+            for (int i = tid - 32; i < 256; i += kTcNT - 32) hn[i] = 0;
+        }
+        __syncthreads();
+        kk -= sel[1];
+        prefix |= (uint32_t)sel[0] << shift;
+        mask |= 255u << shift;
+    }
+    *n_gt = K - kk;
+    return prefix;
+}
+
+// Exclusive prefix counts of two flags in candidate order: f0 of candidate tid (an old
+// row) and f1 of the new-row candidate tid, which follows every old row.  p0 / p1: the set
+// flags before this thread's candidates; t0: the set f0 flags; t: all set flags.
+__device__ __forceinline__ void block_scan_pair(bool f0, bool f1, int* cnt, int& p0, int& p1, int& t0, int& t) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t b0 = __ballot_sync(0xffffffffu, f0), b1 = __ballot_sync(0xffffffffu, f1);
+    if (lane == 0) {
+        cnt[warp] = __popc(b0);
+        cnt[8 + warp] = __popc(b1);
+    }
     __syncthreads();
-    const int col = tid & 15, pr = tid >> 4;
-    float s = 0.f;
-#pragma unroll 8
-    for (int q = 0; q < 16; ++q) s = add_up<C>(s, tr[(pr * 16 + q) * kTcTrLD + col]);
-    part[pr * 16 + col] = s;
-    __syncthreads();
-    float t = 0.f;
-    if (tid < 16)
-        for (int p = 0; p < kTcNT / 16; ++p) t = add_up<C>(t, part[p * 16 + tid]);
-    return t;
+    int a0 = 0, a1 = 0, c0 = 0, c1 = 0;
+#pragma unroll
+    for (int w = 0; w < kTcNT / 32; ++w) {
+        const int x0 = cnt[w], x1 = cnt[8 + w];
+        a0 += w < warp ? x0 : 0;
+        a1 += w < warp ? x1 : 0;
+        c0 += x0;
+        c1 += x1;
+    }
+    const uint32_t lt = (1u << lane) - 1u;
+    p0 = a0 + __popc(b0 & lt);
+    p1 = c0 + a1 + __popc(b1 & lt);
+    t0 = c0;
+    t = c0 + c1;
+    __syncthreads();   // the counts may be rewritten by the next call
 }
 
 template <bool C>
 __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     extern __shared__ __align__(1024) float smem[];
     float* tr = smem + kTcOffTr;
-    float* part = smem + kTcOffPart;
     float* s_base = smem + kTcOffVec;
     float* s_err = s_base + 256;
-    float* s_S = s_err + 256;
-    float* s_alpha = s_S + 256;
-    float* s_delta = s_alpha + 256;
-    float* s_drop = s_delta + 256;
-    float* s_rho = s_drop + 256;    // rounding bound of the layer's dot products, per neuron
+    float* s_alpha = s_err + 256;
+    float* s_rho = s_alpha + 256;   // rounding bound of the layer's dot products, per neuron
     float* s_fold = s_rho + 256;    // per input k: the bound's share before |A| (conservative)
-    float* s_mag = smem + kTcOffMag;
-    int* s_rank = reinterpret_cast<int*>(smem + kTcOffRank);
+    float* s_aout = smem + kTcOffOut;                                   // output layer's column
+    int* s_cnt = reinterpret_cast<int*>(smem + kTcOffOut + 256);        // 16 scan counts
+    int* s_sel = s_cnt + 16;                                            // select: digit, keys above
+    int* s_newj = reinterpret_cast<int*>(smem + kTcOffNew);             // kept new rows: neuron
+    float* s_newd = smem + kTcOffNew + 256;                             //                delta
+    int* hist = reinterpret_cast<int*>(smem + 2048);                    // in the idle stage buffers
     __shared__ NiqSpecHeader H;
     __shared__ __align__(8) uint64_t bar[kTcStages];
     __shared__ uint32_t s_tmem;
@@ -253,11 +328,14 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             __syncthreads();
             tc::fence_after_sync();
         }
-        int nrows = v;
+        int nrows = v;      // noise rows of the layer input: n_old from the scratch, then the new ones
+        int n_old = v;      // rows of X held in the scratch (the rest are diag(delta) rows, built while staging)
+        float out_part = 0.f;   // |output-layer product| of this thread's kept rows (last hidden layer)
 
         for (int li = 0; li + 1 < nL && !fail; ++li) {
             const NiqLayer L = H.layers[li];
             const int out = L.out, o16 = round16(out);
+            const bool last_hidden = (li + 2 == nL);
             // ---------------- dense: noise rows on the tensor cores, base/err on CUDA cores
             if (li > 0) {
                 const int i16 = round16(L.in);
@@ -267,7 +345,22 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 const float* wlo = whi + (long long)chunks * o16 * kTcKC;
                 const uint32_t idesc = tc::idesc_tf32(128, o16);
                 float g_bs = 0.f, g_es = 0.f, g_rho = 0.f;   // column tid of the base, err, rounding rows
-                // chunk c goes to stage c % kTcStages; loads run two chunks ahead of the MMAs
+                // X of a chunk in this thread's float4 slots q (the chunk's float4 tid + 256 q):
+                // row 8 (tid / 32) + tid % 8 + 64 q, inputs 16 c + 4 ((tid / 8) % 4) .. + 3 (the
+                // K-major core-matrix layout).  Rows below n_old come from the scratch, fetched into
+                // registers one chunk ahead; the new rows diag(delta) are built from their neuron
+                // and delta; rows past nrows are zero.
+                float4 pf[4];
+                const int slots = 2 * mt;
+                auto row_of = [&](int q) { return 8 * (tid >> 5) + (tid & 7) + 64 * q; };
+                auto fetch_x = [&](int c) {
+                    if (c >= chunks) return;
+                    const float4* src = reinterpret_cast<const float4*>(xs + c * kTcRows * kTcKC);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (q < slots && row_of(q) < n_old) pf[q] = __ldcg(src + tid + 256 * q);
+                };
+                // chunk c goes to stage c % kTcStages; staging runs two chunks ahead of the MMAs
                 auto load_chunk = [&](int c) {
                     if (c < chunks) {
                         const int s = c % kTcStages;
@@ -276,19 +369,30 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     if (c < chunks && !fail) {   // no copy into a stage whose MMAs may still read it
                         const int s = c % kTcStages;
                         float* stg = smem + s * kTcStage;
-                        const int xf4 = mt * 128 * kTcKC / 4, wf4 = o16 * kTcKC / 4;
-                        const float* xsrc = xs + c * kTcRows * kTcKC;
+                        const int wf4 = o16 * kTcKC / 4;
                         const float* wsrc_h = whi + (long long)c * o16 * kTcKC;
                         const float* wsrc_l = wlo + (long long)c * o16 * kTcKC;
-                        // X is kept once in fp32 and split here: half the scratch traffic of
-                        // keeping hi and lo (the split weights stream with cp.async)
-                        for (int i = tid; i < xf4; i += kTcNT) {
-                            const float4 v = __ldcg(reinterpret_cast<const float4*>(xsrc) + i);
-                            const float4 h = make_float4(tc::tf32_hi(v.x), tc::tf32_hi(v.y), tc::tf32_hi(v.z),
-                                                         tc::tf32_hi(v.w));
+                        const int k0 = c * kTcKC + 4 * ((tid >> 3) & 3);
+                        // X is kept once in fp32 and split here (the split weights stream with cp.async)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            if (q >= slots) break;
+                            const int r = row_of(q);
+                            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (r < n_old) {
+                                x = pf[q];
+                            } else if (r < nrows) {
+                                const int jn = s_newj[r - n_old];
+                                const float dn = s_newd[r - n_old];
+                                x = make_float4(jn == k0 ? dn : 0.f, jn == k0 + 1 ? dn : 0.f, jn == k0 + 2 ? dn : 0.f,
+                                                jn == k0 + 3 ? dn : 0.f);
+                            }
+                            const float4 h = make_float4(tc::tf32_hi(x.x), tc::tf32_hi(x.y), tc::tf32_hi(x.z),
+                                                         tc::tf32_hi(x.w));
+                            const int i = tid + 256 * q;
                             *reinterpret_cast<float4*>(stg + 4 * i) = h;
                             *reinterpret_cast<float4*>(stg + kTcRows * kTcKC + 4 * i) =
-                                make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+                                make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
                         }
                         for (int i = tid; i < wf4; i += kTcNT) {
                             cp_async16(stg + 2 * kTcRows * kTcKC + 4 * i, wsrc_h + 4 * i);
@@ -297,8 +401,11 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     }
                     cp_async_commit();   // an empty group past the last chunk keeps the count
                 };
+                fetch_x(0);
                 load_chunk(0);
+                fetch_x(1);
                 load_chunk(1);
+                fetch_x(2);
                 for (int c = 0; c < chunks; ++c) {
                     const int s = c % kTcStages;
                     float* stg = smem + s * kTcStage;
@@ -329,8 +436,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     }
                     if (!fail) pending |= 1u << s;
                     // the stage of chunk c + 2 held chunk c - 1: every thread finished with it
-                    // (the barrier above); its MMAs are waited for inside load_chunk
+                    // (the barrier above); its MMAs are waited for inside load_chunk.  The X of
+                    // chunk c + 2 was fetched an iteration ago; the next fetch covers the MMAs.
                     load_chunk(c + 2);
+                    fetch_x(c + 3);
                     // base, err and rounding rows while the tensor cores work
                     // (src/affine_layers.py:11-31): column j of the staged weight chunk,
                     // hi + lo = the fp32 weight exactly, against the chunk's 16 inputs
@@ -380,26 +489,34 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 }
             }
             // ---------------- activation epilogue (src/affine.py:164-193)
+            // Thread tid owns noise row tid (TMEM lane tid % 128 of tile tid / 128) and neuron tid.
+            // The stage buffers are idle until the next layer's first copy: they hold the
+            // per-warp column sums and the selection histograms meanwhile.
             const bool row_ok = row < nrows;
-            const bool warp_on = (tile * 128 + (warp & 3) * 32) < nrows;
+            const bool warp_on = warp * 32 < nrows;   // warp-uniform: the warp holds rows of the box
+            const int nw_on = (nrows + 31) >> 5;
             const int nch = (o16 + 31) / 32;
-            // 1. column sums of |D|
-            for (int ch = 0; ch < nch; ++ch) {
-                float val[32];
-                if (warp_on) tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
+            float* wsum = smem;                        // [8 warps][256 columns]
+            float* wt = tr + warp * 32 * kTcTrLD;      // this warp's transpose tile
+            if (last_hidden && tid < out) s_aout[tid] = a.M.w[H.layers[li + 1].a_off + tid * H.layers[li + 1].out_pad];
+            // 1. column sums of |D|: per warp over its 32 rows, then over the warps
+            if (warp_on) {
+                for (int ch = 0; ch < nch; ++ch) {
+                    float val[32];
+                    tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) val[i] = (warp_on && row_ok && ch * 32 + i < out) ? fabsf(val[i]) : 0.f;
-                const float t0 = column_sum16<C>(val, row, tr, part);
-                if (tid < 16) s_S[ch * 32 + tid] = t0;
-                const float t1 = column_sum16<C>(val + 16, row, tr, part);
-                if (tid < 16) s_S[ch * 32 + 16 + tid] = t1;
+                    for (int i = 0; i < 32; ++i) val[i] = (row_ok && ch * 32 + i < out) ? fabsf(val[i]) : 0.f;
+                    wsum[warp * 256 + ch * 32 + lane] = warp_column_sum32<C>(val, wt, lane);
+                }
             }
             __syncthreads();
             // 2. linearisation per column
             const int j = tid;
             float nb = 0.f, e = 0.f, aS = 0.f, alpha = 0.f, delta = 0.f;
             if (j < out) {
-                const float base = s_base[j], err = s_err[j], S = s_S[j];
+                float S = 0.f;
+                for (int w = 0; w < nw_on; ++w) S = add_up<C>(S, wsum[w * 256 + j]);
+                const float base = s_base[j], err = s_err[j];
                 const float rad = add_up<C>(add_up<C>(S, err), s_rho[j]);
                 const float lo = sub_dn<C>(base, rad), hi = add_up<C>(base, rad);
                 const Lin z = linearize<C>(L.act, lo, hi);
@@ -414,77 +531,109 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     delta = __fmaf_ru(__fadd_ru(fabsf(nb), aS), NIQ_ULP_REL, delta);
                 }
             }
-            if (j < NIQ_MAX_WIDTH) { s_alpha[j] = alpha; s_delta[j] = delta; }
+            if (j < NIQ_MAX_WIDTH) s_alpha[j] = alpha;   // 0 past the layer's width
             __syncthreads();
-            // 3. magnitudes of the candidate rows: scaled old rows, then the new rows
+            // 3. magnitudes of the candidate rows (src/affine.py:141-142): the scaled old rows
+            //    (thread = row) and the new rows diag(delta) (thread = neuron)
             const int ncand = nrows + out;
             const bool truncate = mode == NIQ_MODE_AFFINE_TRUNCATE && ncand > K;
+            bool keep0 = row_ok, keep1 = j < out;
             if (truncate) {
                 float m = 0.f;
-                for (int ch = 0; ch < nch; ++ch) {
-                    float val[32];
-                    if (warp_on) tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
+                if (warp_on) {
+                    for (int ch = 0; ch < nch; ++ch) {
+                        float val[32];
+                        tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i)
-                        m += (warp_on && ch * 32 + i < out) ? fabsf(__fmul_rn(s_alpha[ch * 32 + i], val[i])) : 0.f;
-                }
-                if (row_ok) s_mag[row] = m;
-                if (j < out) s_mag[nrows + j] = delta;
-                __syncthreads();
-                // 4. stable descending rank
-                if (row_ok) s_rank[row] = stable_rank(s_mag, ncand, m, row, row - lane);
-                if (j < out) s_rank[nrows + j] = stable_rank(s_mag, ncand, delta, nrows + j, nrows + j - lane);
-            } else {
-                if (row_ok) s_rank[row] = row;
-                if (j < out) s_rank[nrows + j] = nrows + j;
-            }
-            __syncthreads();
-            const int keep = truncate ? K : ncand;
-            // 5. write the kept rows as the next X (split), fold the dropped ones
-            const int my_rank = row_ok ? s_rank[row] : kTcRows;
-            const bool kept = row_ok && my_rank < keep;
-            for (int ch = 0; ch < nch; ++ch) {
-                float val[32];
-                if (warp_on) tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
+                        for (int i = 0; i < 32; i += 4) {
+                            const float4 al = *reinterpret_cast<const float4*>(s_alpha + ch * 32 + i);
+                            const float a4[4] = {al.x, al.y, al.z, al.w};
 #pragma unroll
-                for (int i = 0; i < 32; ++i)
-                    val[i] = (warp_on && ch * 32 + i < out) ? __fmul_rn(s_alpha[ch * 32 + i], val[i]) : 0.f;
-                if (kept) {
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const int k = ch * 32 + 4 * q;
-                        if (k >= o16) break;
-                        *reinterpret_cast<float4*>(xs + x_index(my_rank, k)) =
-                            make_float4(val[4 * q], val[4 * q + 1], val[4 * q + 2], val[4 * q + 3]);
+                            for (int u = 0; u < 4; ++u)
+                                m += (ch * 32 + i + u < out) ? fabsf(__fmul_rn(a4[u], val[i + u])) : 0.f;
+                        }
                     }
                 }
-#pragma unroll
-                for (int i = 0; i < 32; ++i) val[i] = (row_ok && !kept) ? fabsf(val[i]) : 0.f;
-                const float t0 = column_sum16<C>(val, row, tr, part);
-                if (tid < 16) s_drop[ch * 32 + tid] = t0;
-                const float t1 = column_sum16<C>(val + 16, row, tr, part);
-                if (tid < 16) s_drop[ch * 32 + 16 + tid] = t1;
+                // 4. keep the K largest (src/affine.py:150-155): the K-th largest magnitude T by a
+                //    radix select; every candidate above T and the first candidates equal to T, in
+                //    candidate order (old rows, then new rows), as a stable descending sort keeps them
+                const uint32_t k0 = __float_as_uint(m), k1 = __float_as_uint(delta);
+                int n_gt;
+                const uint32_t T = block_kth_largest(k0, row_ok, k1, j < out, K, hist, s_sel, &n_gt);
+                int q0, q1, t0, tt;
+                block_scan_pair(row_ok && k0 == T, j < out && k1 == T, s_cnt, q0, q1, t0, tt);
+                keep0 = row_ok && (k0 > T || (k0 == T && q0 < K - n_gt));
+                keep1 = j < out && (k1 > T || (k1 == T && q1 < K - n_gt));
             }
-            // new rows diag(delta): kept ones become rows of X, dropped ones go to err
+            // kept rows are packed in candidate order: old rows to 0 .. n_keep_old - 1, new after
+            int p0, p1, n_keep_old, keep;
+            block_scan_pair(keep0, keep1, s_cnt, p0, p1, n_keep_old, keep);
+            // 5. kept old rows, scaled by alpha, become the next X (or, after the last hidden
+            //    layer, their products with the output layer's column); dropped rows go to err
+            //    as column sums of |alpha D| (src/affine.py:157-160)
+            float d_out = 0.f;
+            if (warp_on) {
+                const bool any_drop = __any_sync(0xffffffffu, row_ok && !keep0);
+                for (int ch = 0; ch < nch; ++ch) {
+                    float val[32];
+                    tc::tmem_ld32(t_row + (uint32_t)(ch * 32), val);
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4) {
+                        const float4 al = *reinterpret_cast<const float4*>(s_alpha + ch * 32 + i);
+                        const float a4[4] = {al.x, al.y, al.z, al.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            val[i + u] = (ch * 32 + i + u < out) ? __fmul_rn(a4[u], val[i + u]) : 0.f;
+                    }
+                    if (keep0) {
+                        if (last_hidden) {
+#pragma unroll
+                            for (int i = 0; i < 32; ++i)
+                                if (ch * 32 + i < out) d_out = fmaf(val[i], s_aout[ch * 32 + i], d_out);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const int k = ch * 32 + 4 * q;
+                                if (k >= o16) break;
+                                *reinterpret_cast<float4*>(xs + x_index(p0, k)) =
+                                    make_float4(val[4 * q], val[4 * q + 1], val[4 * q + 2], val[4 * q + 3]);
+                            }
+                        }
+                    }
+                    if (any_drop) {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) val[i] = (row_ok && !keep0) ? fabsf(val[i]) : 0.f;
+                        wsum[warp * 256 + ch * 32 + lane] = warp_column_sum32<C>(val, wt, lane);
+                    } else {
+                        wsum[warp * 256 + ch * 32 + lane] = 0.f;
+                    }
+                }
+            }
+            // new rows diag(delta): kept ones are built into X while the next layer stages it,
+            // dropped ones go to err
+            float d_new = 0.f;
             if (j < out) {
-                const int rk = s_rank[nrows + j];
-                if (rk < keep) {
-                    for (int k = 0; k < o16; k += 4)
-                        *reinterpret_cast<float4*>(xs + x_index(rk, k)) =
-                            make_float4(j == k ? delta : 0.f, j == k + 1 ? delta : 0.f, j == k + 2 ? delta : 0.f,
-                                        j == k + 3 ? delta : 0.f);
+                if (keep1) {
+                    if (last_hidden) d_new = __fmul_rn(delta, s_aout[j]);
+                    else {
+                        s_newj[p1 - n_keep_old] = j;
+                        s_newd[p1 - n_keep_old] = delta;
+                    }
                 } else {
                     e = add_up<C>(e, delta);
                 }
             }
+            if (last_hidden) out_part = add_up<C>(keep0 ? fabsf(d_out) : 0.f, keep1 ? fabsf(d_new) : 0.f);
             __syncthreads();
             // 6. err of the activation output, with the next layer's rounding folded in
             float fold = 0.f;
             if (j < out) {
-                e = add_up<C>(e, s_drop[j]);
+                float drop = 0.f;
+                for (int w = 0; w < nw_on; ++w) drop = add_up<C>(drop, wsum[w * 256 + j]);
+                e = add_up<C>(e, drop);
                 if (C) {
                     const NiqLayer& Ln = H.layers[li + 1];
-                    if (li + 2 < nL)  // next layer: noise rows on the tensor cores, base on the CUDA cores
+                    if (!last_hidden)  // next layer: noise rows on the tensor cores, base on the CUDA cores
                         fold = __fmaf_ru(gamma_tc(Ln.in), __fadd_ru(aS, delta), __fmul_ru(Ln.gamma, fabsf(nb)));
                     else
                         fold = __fmul_ru(Ln.gamma, __fadd_ru(__fadd_ru(fabsf(nb), aS), delta));
@@ -496,6 +645,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 s_fold[j] = fold;
             }
             nrows = keep;
+            n_old = n_keep_old;
             // X written by this layer visible to the next layer's copies; TMEM reads done
             // before the next layer's MMAs overwrite it
             __threadfence_block();
@@ -504,33 +654,46 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             tc::fence_after_sync();
         }
         if (fail) break;
-        // ---------------- last layer (one output) on the CUDA cores
+        // ---------------- last layer (one output) on the CUDA cores: its noise-row products
+        // came out of the last hidden layer's epilogue (out_part); base, err and rounding
+        // rows as dot products over the layer's inputs
         {
             const NiqLayer L = H.layers[nL - 1];
             const float* A = a.M.w + L.a_off;
             const float gam = C ? L.gamma : 0.f;
-            float part_s = 0.f;
-            if (row < nrows) {
-                float d = 0.f;
-                for (int k = 0; k < L.in; k += 4) {
-                    const int xi = x_index(row, k);
-                    const float4 xv = *reinterpret_cast<const float4*>(xs + xi);
-                    const float x4[4] = {xv.x, xv.y, xv.z, xv.w};
-                    for (int q = 0; q < 4 && k + q < L.in; ++q) d = fmaf(x4[q], A[(k + q) * L.out_pad], d);
-                }
-                part_s = fabsf(d);
+            float pb = 0.f, pe = 0.f, pr = 0.f;
+            if (tid < L.in) {
+                const float w = A[tid * L.out_pad];
+                pb = __fmul_rn(s_base[tid], w);
+                pe = C ? __fmul_ru(s_err[tid], fabsf(w)) : __fmul_rn(s_err[tid], fabsf(w));
+                if (C) pr = __fmul_ru(s_fold[tid], fabsf(w));
             }
-            const float S = wide_block_sum<C>(part_s, red);
+            // warp sums, then thread 0 adds the warps' (rounded up where conservative; the base
+            // row is rounded to nearest, its rounding is in rho)
+            float v4[4] = {out_part, pb, pe, pr};
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float y = __shfl_down_sync(0xffffffffu, v4[q], off);
+                    v4[q] = q == 1 ? v4[q] + y : add_up<C>(v4[q], y);
+                }
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) red[8 * q + warp] = v4[q];
+            }
+            __syncthreads();
             if (tid == 0) {
-                float bs = 0.f, es = 0.f, rho = 0.f;
-                for (int k = 0; k < L.in; ++k) {
-                    const float w = A[k * L.out_pad];
-                    bs = fmaf(s_base[k], w, bs);
-                    es = fmaf(s_err[k], fabsf(w), es);
-                    if (C) rho = __fmaf_ru(s_fold[k], fabsf(w), rho);
+                float S = 0.f, bs0 = 0.f, es0 = 0.f, rho0 = 0.f;
+                for (int w = 0; w < kTcNT / 32; ++w) {
+                    S = add_up<C>(S, red[w]);
+                    bs0 += red[8 + w];
+                    es0 = add_up<C>(es0, red[16 + w]);
+                    rho0 = add_up<C>(rho0, red[24 + w]);
                 }
                 const float bj = a.M.w[L.b_off];
-                bs = __fadd_rn(bs, bj);
+                const float bs = __fadd_rn(bs0, bj);
+                float es = es0, rho = rho0;
                 if (C) {
                     es = __fmul_ru(es, 1.f + 2.f * gam);
                     rho = __fadd_ru(__fmaf_ru(rho, 1.f + 2.f * gam, __fmul_ru(gam, fabsf(bj))), (float)(L.in + 2) * NIQ_TINY);
@@ -540,7 +703,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 a.sign_out[b] = sign_of_bounds(lo, hi, a.offset);
                 if (a.lohi_out) { a.lohi_out[2 * b] = lo; a.lohi_out[2 * b + 1] = hi; }
             }
-            __syncthreads();
+            __syncthreads();   // red is rewritten by the next box
         }
     }
     // unwind: wait (bounded) for MMAs still in flight, then free TMEM

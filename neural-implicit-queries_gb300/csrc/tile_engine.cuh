@@ -11,6 +11,8 @@
 //   ROWS_SLOPE  (R=8, NABS=4): 0 primal | 1..v slope centers | v+1..v+np points |
 //       4 primal rounding error | 5..4+v slope widths      (src/slope_interval.py:164-210)
 //   ROWS_POINTS (NABS=0): every row is a point evaluation (src/mlp.py:253-347)
+//   ROWS_JVP    (NABS=0, R=8): two points, each a value row and three tangent rows
+//       (d/dx, d/dy, d/dz): forward-mode derivatives, jax.jacfwd of src/render.py:61-63
 //
 // Dense rule (src/affine_layers.py:11-31, src/slope_interval_layers.py:11-33):
 //   base <- base@A + b, aff <- aff@A, err <- err@|A|.
@@ -32,7 +34,7 @@
 
 namespace niq {
 
-enum RowMode : int { ROWS_AFFINE = 0, ROWS_SLOPE = 1, ROWS_POINTS = 2 };
+enum RowMode : int { ROWS_AFFINE = 0, ROWS_SLOPE = 1, ROWS_POINTS = 2, ROWS_JVP = 3 };
 
 struct RowPlan {
     int mode;  // RowMode
@@ -225,6 +227,16 @@ __device__ __forceinline__ float act_point(int act, float x) {
     if (act == NIQ_ACT_ELU) return elu_f(x);
     if (act == NIQ_ACT_TANH) return tanhf(x);
     return x;
+}
+
+// Derivative of the activation at x, given y = act(x), as JAX differentiates it:
+// relu' = 1 where x > 0 else 0 (jax.nn.relu), elu' = 1 where x > 0 else exp(x)
+// (jax.nn.elu), tanh' = 1 - tanh(x)^2.
+__device__ __forceinline__ float act_deriv(int act, float x, float y) {
+    if (act == NIQ_ACT_RELU) return x > 0.f ? 1.f : 0.f;
+    if (act == NIQ_ACT_ELU) return x > 0.f ? 1.f : expf(x);
+    if (act == NIQ_ACT_TANH) return __fsub_rn(1.f, __fmul_rn(y, y));
+    return 1.f;
 }
 
 // Derivative bounds of the activation over [pl, pu] for slope intervals
@@ -558,6 +570,18 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                 if (plan.mode == ROWS_POINTS) {
 #pragma unroll
                     for (int r = 0; r < R; ++r) v[r] = act_point(act, __fadd_rn(v[r], b));
+                } else if (NABS == 0 && plan.mode == ROWS_JVP) {
+                    // value rows 0 and 4 get the bias and the activation; their tangent rows
+                    // the activation's derivative at the pre-activation
+#pragma unroll
+                    for (int p0 = 0; p0 + 3 < R; p0 += 4) {
+                        const float pre = __fadd_rn(v[p0], b);
+                        const float y = act_point(act, pre);
+                        const float d = act_deriv(act, pre, y);
+                        v[p0] = y;
+#pragma unroll
+                        for (int r = p0 + 1; r < p0 + 4; ++r) v[r] = __fmul_rn(d, v[r]);
+                    }
                 } else if (plan.mode == ROWS_AFFINE) {
                     float base = __fadd_rn(v[0], b);
                     float err = v[R - 1];

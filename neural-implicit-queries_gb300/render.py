@@ -55,11 +55,12 @@ def look_at(eye_pos, target=None, up_dir='y'):
 
 
 def outward_normals(funcs_tuple, params_tuple, hit_pos, hit_ids, eps, method='finite_differences'):
-    """src/render.py:53-90: (N, 3) unit normals by tetrahedron central differences of the
-    function each point hit (hit id 1-based; zeros where none).  Device tensors in give
-    device tensors out."""
-    if method != 'finite_differences':
-        raise ValueError("only method='finite_differences' is supported (autodiff needs JAX)")
+    """src/render.py:53-90: (N, 3) unit normals of the function each point hit (hit id
+    1-based; zeros where none).  'finite_differences': tetrahedron central differences;
+    'autodiff': the normalised exact gradient (forward-mode derivatives on the device, the
+    jax.jacfwd of the reference).  Device tensors in give device tensors out."""
+    if method not in ('finite_differences', 'autodiff'):
+        raise ValueError("unrecognized method")
     if not isinstance(funcs_tuple, (tuple, list)):
         funcs_tuple, params_tuple = (funcs_tuple,), (params_tuple,)
     t = _io.require_cuda()
@@ -71,21 +72,47 @@ def outward_normals(funcs_tuple, params_tuple, hit_pos, hit_ids, eps, method='fi
     n = pos.shape[0]
     out = t.empty((n, 3), dtype=t.float32, device='cuda')
     L = _lib.load()
+    handles = (_lib.C.c_void_p * len(models))(*[m.handle.value for m in models])
+    if method == 'autodiff':
+        ws_bytes = L.niq_outward_normals_autodiff_workspace_size(n)
+        ws = _io.workspace(ws_bytes)
+        _lib.check(L.niq_outward_normals_autodiff(handles, len(models), n, _io.ptr(pos), _io.ptr(hid.reshape(-1)),
+                                                  _io.ptr(out), _io.ptr(ws), ws_bytes, _io.stream_handle()))
+        return _io.back(out, kind)
     ws_bytes = L.niq_outward_normals_workspace_size(n)
     ws = _io.workspace(ws_bytes)
-    handles = (_lib.C.c_void_p * len(models))(*[m.handle.value for m in models])
     _lib.check(L.niq_outward_normals(handles, len(models), n, _io.ptr(pos), _io.ptr(hid.reshape(-1)), float(eps),
                                      _io.ptr(out), _io.ptr(ws), ws_bytes, _io.stream_handle()))
     return _io.back(out, kind)
+
+
+def _shading_colors(fn, hit_pos, hit_ids, n):
+    """(n, 3) float32 colors of ``fn`` at the hit positions (white where nothing was hit,
+    which the shading replaces by the background)."""
+    pos = np.asarray(_io.to_numpy(hit_pos), np.float32).reshape(-1, 3)
+    hit = np.asarray(_io.to_numpy(hit_ids)).reshape(-1) > 0
+    out = np.ones((n, 3), np.float32)
+    if not hit.any():
+        return out
+    sel = pos[hit]
+    try:
+        cols = np.asarray(fn(sel), np.float32)
+        if cols.shape != (sel.shape[0], 3):
+            raise ValueError
+    except Exception:
+        cols = np.stack([np.asarray(fn(p), np.float32).reshape(3) for p in sel])
+    out[hit] = cols
+    return out
 
 
 def shade_image(shading, ray_dirs, hit_pos, hit_normals, hit_ids, up_dir, matcaps, shading_color_tuple,
                 shading_color_func=None, tonemap=False):
     """src/render.py:161-224 (plus the white background of :139 and, optionally,
     tonemap_image): (N, 3) colors.  ``matcaps`` is the (r, g, b, k) tuple of (H, W, 3)
-    images; ``shading_color_func`` (a Python callable) is not supported on the device."""
-    if shading_color_func is not None:
-        raise NotImplementedError("shading_color_func runs Python per pixel; pass shading_color_tuple")
+    images.  ``shading_color_func`` (a callable of a hit position, as the reference
+    vmaps it) gives each hit pixel its color in place of ``shading_color_tuple``: it runs
+    on the host over the hit positions (once on the whole (N, 3) array if it accepts one,
+    else per position) and the colors go to the device with the matcap shading."""
     t = _io.require_cuda()
     dirs, kind = _io.to_dev(ray_dirs)
     nrm, _ = _io.to_dev(hit_normals)
@@ -112,6 +139,12 @@ def shade_image(shading, ray_dirs, hit_pos, hit_normals, hit_ids, up_dir, matcap
         ncol = colf.shape[0]
     else:
         raise RuntimeError("Unrecognized shading parameter")
+    if shading_color_func is not None and code == 1:
+        pix = t.from_numpy(_shading_colors(shading_color_func, hit_pos, hit_ids, n)).cuda()
+        _lib.check(L.niq_shade_image_pixel_colors(n, _io.ptr(dirs.reshape(-1, 3)), _io.ptr(nrm.reshape(-1, 3)),
+                                                  _io.ptr(hid.reshape(-1)), up, _io.ptr(mc), mh, mw, _io.ptr(pix),
+                                                  1 if tonemap else 0, _io.ptr(out), _io.stream_handle()))
+        return _io.back(out, kind)
     _lib.check(L.niq_shade_image(code, n, _io.ptr(dirs.reshape(-1, 3)), _io.ptr(nrm.reshape(-1, 3)),
                                  _io.ptr(hid.reshape(-1)), up, _io.ptr(mc) if mc is not None else None, mh, mw, cols,
                                  ncol, 1 if tonemap else 0, _io.ptr(out), _io.stream_handle()))
@@ -153,7 +186,8 @@ def render_image(funcs_tuple, params_tuple, eye_pos, look_dir, up_dir, left_dir,
     dt = t.from_numpy(dirs).cuda()
     hit_pos = rt + tt[:, None] * dt
     normals = outward_normals(funcs_tuple, params_tuple, hit_pos, hit, opts['hit_eps'])
-    img = shade_image(shading, dt, hit_pos, normals, hit, up_dir, matcaps, shading_color_tuple, tonemap=tonemap)
+    img = shade_image(shading, dt, hit_pos, normals, hit, up_dir, matcaps, shading_color_tuple,
+                      shading_color_func=shading_color_func, tonemap=tonemap)
     img = img.reshape(res, res, 3).cpu().numpy()
     return (img, tt.reshape(res, res).cpu().numpy(), cnt.reshape(res, res).cpu().numpy(),
             hit.reshape(res, res).cpu().numpy(), n_eval, -1)

@@ -119,6 +119,38 @@ def eval_points(params, x, dtype=np.float32):
     return x
 
 
+def eval_gradients(params, x, dtype=np.float32):
+    """Value and gradient of the MLP at points ``x`` (N, 3) -> ((N,), (N, 3)): forward-mode
+    tangents, as jax.jacfwd of the point function (src/render.py:61-63).  The activation
+    derivatives are those JAX differentiates: relu' = 1 where x > 0 else 0 (jax.nn.relu),
+    elu' = 1 where x > 0 else exp(x) (jax.nn.elu), tanh' = 1 - tanh(x)^2."""
+    x = np.asarray(x, dtype=dtype)
+    t = np.broadcast_to(np.eye(3, dtype=dtype), x.shape[:-1] + (3, 3)).copy()   # d x / d input, (N, 3 tangents, 3)
+    for op in spec_ops(params, dtype):
+        name = op[0]
+        if name == 'dense':
+            _, A, b = op
+            x = x @ A
+            t = t @ A
+            if b is not None:
+                x = x + b
+        elif name == 'relu':
+            d = (x > 0).astype(dtype)
+            x = np.maximum(x, 0)
+            t = t * d[..., None, :]
+        elif name == 'elu':
+            d = np.where(x > 0, dtype(1), np.exp(np.minimum(x, 0))).astype(dtype)
+            x = _elu(x)
+            t = t * d[..., None, :]
+        elif name == 'tanh':
+            x = np.tanh(x)
+            t = t * (1 - x * x)[..., None, :]
+        elif name == 'squeeze_last':
+            x = x[..., 0]
+            t = t[..., 0]
+    return x, t
+
+
 # ----------------------------------------------------------------------------------------
 # Affine arithmetic  (src/affine.py, src/affine_layers.py)
 # ----------------------------------------------------------------------------------------
@@ -850,11 +882,20 @@ def cast_rays_frustum(funcs, params_list, cam_params, opts, trace=False):
 _TET = np.array(((1., -1., -1.), (-1., -1., 1.), (-1., 1., -1.), (1., 1., 1.)), np.float32)
 
 
-def outward_normals(funcs, params_list, hit_pos, hit_ids, eps):
-    """src/render.py:53-90 ('finite_differences'): tetrahedron central differences,
-    normalised, of the function each point hit; zeros where none."""
+def outward_normals(funcs, params_list, hit_pos, hit_ids, eps, method='finite_differences'):
+    """src/render.py:53-90: the normalised gradient of the function each point hit, zeros
+    where none.  'finite_differences': tetrahedron central differences; 'autodiff': the
+    exact gradient (jax.jacfwd, here forward-mode tangents, eval_gradients)."""
     f32 = funcs[0].dtype
     hit_pos = np.asarray(hit_pos, f32)
+    if method == 'autodiff':
+        out = np.zeros_like(hit_pos)
+        for fid, params in enumerate(params_list, start=1):
+            _, grad = eval_gradients(params, hit_pos, f32)
+            out = np.where((hit_ids == fid)[:, None], normalize(grad.astype(f32)).astype(f32), out)
+        return out
+    if method != 'finite_differences':
+        raise ValueError("unrecognized method")
     offsets = (_TET * np.asarray(eps, f32)).astype(f32)
     out = np.zeros_like(hit_pos)
     for fid, (func, params) in enumerate(zip(funcs, params_list), start=1):
@@ -881,8 +922,10 @@ def _map_coordinates_linear_nearest(img, x, y):
     return acc
 
 
-def shade_image(shading, ray_dirs, hit_normals, hit_ids, up_dir, matcaps, colors):
-    """src/render.py:161-224 plus the white background of :139."""
+def shade_image(shading, ray_dirs, hit_normals, hit_ids, up_dir, matcaps, colors, hit_pos=None,
+                shading_color_func=None):
+    """src/render.py:161-224 plus the white background of :139; ``shading_color_func``
+    (src/render.py:198-206) gives each hit position its color, one position at a time."""
     f32 = np.float32
     n = np.asarray(hit_normals, f32)
     if shading == 'normal':
@@ -899,8 +942,13 @@ def shade_image(shading, ray_dirs, hit_normals, hit_ids, up_dir, matcaps, colors
         x = ((u + 1.) / 2. * H).astype(f32)
         y = ((-v + 1.) / 2. * W).astype(f32)
         cols = np.ones((n.shape[0], 3), f32)
-        for fid, col in enumerate(colors, start=1):
-            cols = np.where((hit_ids == fid)[:, None], np.asarray(col, f32)[None], cols)
+        if shading_color_func is not None:
+            pos = np.asarray(hit_pos, f32)
+            for i in np.nonzero(hit_ids > 0)[0]:
+                cols[i] = np.asarray(shading_color_func(pos[i]), f32)
+        else:
+            for fid, col in enumerate(colors, start=1):
+                cols = np.where((hit_ids == fid)[:, None], np.asarray(col, f32)[None], cols)
         ck = (1. - (cols[:, 0] + cols[:, 2] + cols[:, 1])).astype(f32)
         c = np.zeros((n.shape[0], 3), f32)
         for ch in range(3):

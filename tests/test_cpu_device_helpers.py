@@ -22,22 +22,68 @@ struct float4 { float x, y, z, w; };
 '''
 
 MAIN = r'''
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+// The selection of k_wide_tc on the host: the device's 4-pass radix select (histograms
+// of 8-bit digits, the per-lane digit search over lanes whose 'above' counts are the
+// exclusive prefix over lanes), then the tie rule and the candidate-order packing.
+static uint32_t bits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 int main() {
-    alignas(16) float s[512];
-    long bad = 0, tot = 0;
     srand(7);
-    for (int trial = 0; trial < 300; ++trial) {
-        const int n = 1 + rand() % 512;
-        for (int i = 0; i < n; ++i) s[i] = (rand() % 4 == 0) ? 0.f : (float)(rand() % 9);  // many ties
-        if (trial % 50 == 0) s[rand() % n] = NAN;
-        for (int me = 0; me < n; ++me)
-            for (int lane = 0; lane < 32 && lane <= me; lane += 5) {
-                const float v = s[me];
-                int ref = 0;   // stable descending argsort position
-                for (int i = 0; i < n; ++i) ref += (s[i] > v) || (s[i] == v && i < me);
-                bad += stable_rank(s, n, v, me, me - lane) != ref;
-                ++tot;
+    long bad = 0, tot = 0;
+    for (int trial = 0; trial < 3000; ++trial) {
+        const int n = 2 + rand() % 512;
+        std::vector<float> key(n);
+        const int style = trial % 4;
+        for (int i = 0; i < n; ++i) {
+            if (style == 0) key[i] = (rand() % 4 == 0) ? 0.f : (float)(rand() % 9);            // many ties
+            else if (style == 1) key[i] = ldexpf((float)rand() / RAND_MAX, -(rand() % 60));    // spread exponents
+            else if (style == 2) key[i] = 1.f + (rand() % 3) * 1e-7f;                          // one top digit
+            else key[i] = (float)rand() / RAND_MAX;
+        }
+        if (trial % 97 == 0) key[rand() % n] = INFINITY;
+        const int K = 1 + rand() % (n - 1);
+        // device algorithm
+        uint32_t prefix = 0, mask = 0;
+        int kk = K;
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = 24 - 8 * pass;
+            int h[256] = {0};
+            for (int i = 0; i < n; ++i)
+                if ((bits(key[i]) & mask) == prefix) h[(bits(key[i]) >> shift) & 255u]++;
+            int sel[2] = {-1, -1}, above = 0;
+            for (int lane = 0; lane < 32; ++lane) {
+                int t = 0;
+                for (int e = 0; e < 8; ++e) t += h[255 - 8 * lane - e];
+                kth_digit_in_lane(h, lane, above, kk, sel);
+                above += t;
             }
+            if (sel[0] < 0) { ++bad; break; }
+            kk -= sel[1];
+            prefix |= (uint32_t)sel[0] << shift;
+            mask |= 255u << shift;
+        }
+        const uint32_t T = prefix;
+        const int n_gt = K - kk;
+        std::vector<int> kept(n, 0);
+        int ties = 0;
+        for (int i = 0; i < n; ++i) {
+            const uint32_t b = bits(key[i]);
+            kept[i] = b > T || (b == T && ties < K - n_gt);
+            ties += b == T;
+        }
+        // reference: stable descending argsort, first K
+        std::vector<int> idx(n);
+        for (int i = 0; i < n; ++i) idx[i] = i;
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return key[a] > key[b]; });
+        std::vector<int> ref(n, 0);
+        for (int r = 0; r < K; ++r) ref[idx[r]] = 1;
+        int nk = 0;
+        for (int i = 0; i < n; ++i) { bad += kept[i] != ref[i]; nk += kept[i]; }
+        bad += nk != K;
+        ++tot;
     }
     printf("%ld %ld\n", bad, tot);
     return 0;
@@ -52,17 +98,19 @@ def _function_text(path, signature):
     return src[i:j]
 
 
-def test_stable_rank_matches_naive_count(tmp_path):
-    """k_wide_tc.cu's stable_rank (float4 steps outside the warp's index window) gives the
-    same rank as counting every element with the index tie rule, ties and NaN included."""
+def test_radix_select_keeps_the_stable_top_k(tmp_path):
+    """k_wide_tc.cu's per-lane digit search (kth_digit_in_lane), driven through the four
+    8-bit passes of its block radix select and the tie rule, keeps exactly the rows a stable
+    descending argsort keeps first (src/affine.py:150-155): ties, zeros, spread exponents
+    and infinities included."""
     if shutil.which('g++') is None:
         pytest.skip('g++ not available')
-    fn = _function_text(os.path.join(CSRC, 'k_wide_tc.cu'), '__device__ __forceinline__ int stable_rank')
-    cpp = tmp_path / 'rank.cpp'
+    fn = _function_text(os.path.join(CSRC, 'k_wide_tc.cu'), '__device__ __forceinline__ void kth_digit_in_lane')
+    cpp = tmp_path / 'select.cpp'
     cpp.write_text(SHIM + fn + MAIN)
-    exe = tmp_path / 'rank'
+    exe = tmp_path / 'select'
     subprocess.run(['g++', '-O2', '-o', str(exe), str(cpp)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     bad, tot = int(out[0]), int(out[1])
-    assert tot > 100000
+    assert tot == 3000
     assert bad == 0
