@@ -760,7 +760,7 @@ def run_batched(args):
                       "some_query_spent_budget": budget_hit, "model_generation_s": t_gen}))
 
 
-def make_serving_requests(niq, n, rng, max_res=512, max_points=16384, eps=1e-3, node_budget=4096):
+def make_serving_requests(niq, n, rng, max_res=512, max_points=16384, eps=1e-3, node_budget=64):
     """The serving mix: ray tiles (64^2..max_res^2 from a random camera at distance 3),
     closest-point batches (1..max_points points, log-uniform, eps 1e-3, at most
     ``node_budget`` nodes per query: the models are untrained, their bounds loose, and a
@@ -812,7 +812,8 @@ def run_serve(args):
     for f in [srv.submit(r) for r in warm]:
         f.exception(timeout=600)
     # saturation: everything submitted at once
-    sat = make_serving_requests(niq, args.serve_requests, rng, max_res=args.serve_max_res)
+    sat = make_serving_requests(niq, args.serve_requests, rng, max_res=args.serve_max_res,
+                                node_budget=args.serve_node_budget)
     t0 = time.perf_counter()
     futs = [srv.submit(r) for r in sat]
     errors = sum(1 for f in futs if f.exception(timeout=1800) is not None)
@@ -827,13 +828,15 @@ def run_serve(args):
                                                  "errors": errors, "by_kind": st_sat.get("by_kind"),
                                                  "closest_requests_budget_spent": spent_sat}, "rates": [],
            "config": {"workload": "serving_mix", "impl": args.serve_impl, "lanes": args.serve_lanes,
-                      "closest_point": "eps 1e-3, persistent traversal, 4096 nodes per query; a request whose "
-                                       "query spends the budget is answered with upper bounds and counted",
+                      "closest_point": f"eps 1e-3, persistent traversal, {args.serve_node_budget} nodes per query; "
+                                       "a request whose query spends the budget is answered with upper bounds "
+                                       "and counted",
                       "mix": "45% ray tiles 64^2..512^2, 45% closest-point batches 1..16k points, "
                              "10% intersections under random rigid transforms"}}
     for frac in args.serve_fracs:
         rate = frac * peak
-        reqs = make_serving_requests(niq, max(8, int(rate * args.serve_seconds)), rng, max_res=args.serve_max_res)
+        reqs = make_serving_requests(niq, max(40, int(rate * args.serve_seconds)), rng, max_res=args.serve_max_res,
+                                     node_budget=args.serve_node_budget)
         srv.latencies.clear()
         srv.kind_latencies.clear()
         srv.budget_exhausted = 0
@@ -871,6 +874,9 @@ def main():
     ap.add_argument('--serve-impl', default='native', choices=['native', 'python'],
                     help='the native serving runtime (niq_batch_submit) or the Python scheduler')
     ap.add_argument('--serve-lanes', type=int, default=8)
+    ap.add_argument('--serve-node-budget', type=int, default=64,
+                    help='closest-point nodes per query in the serving mix (untrained networks: a 16k-point batch '
+                         'at eps 1e-3 can need millions of nodes per query without one)')
     ap.add_argument('--n-models', type=int, default=512)
     ap.add_argument('--plain-models', type=int, default=64)
     ap.add_argument('--node-budget', type=int, default=2048,

@@ -308,6 +308,19 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     const size_t need = niq_batched_closest_point_workspace_size(total, n_jobs);
     NIQ_REQUIRE(workspace && workspace_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", need);
     cudaStream_t s = as_stream(stream);
+    // the models the jobs use, in a compact table (at most n_jobs entries, which the
+    // workspace size allows for, however large the caller's table is)
+    std::vector<int> compact(n_models, -1);
+    std::vector<NiqModelRef> refs;
+    std::vector<int> used;
+    for (int j = 0; j < n_jobs; ++j) {
+        const int m = job_model[j];
+        if (compact[m] < 0) {
+            compact[m] = (int)refs.size();
+            refs.push_back(models[m]->ref());
+            used.push_back(m);
+        }
+    }
     // chunks, largest model cost first (longest-processing-time order)
     std::vector<BChunk> chunks;
     std::vector<double> cost;
@@ -318,7 +331,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
         for (int l = 0; l < H.n_layers; ++l) per_q += (double)H.layers[l].in * H.layers[l].out;
         for (long long b = 0; b < query_count[j]; b += chunk_q) {
             BChunk c;
-            c.model = job_model[j];
+            c.model = compact[job_model[j]];
             c.q_begin = (int)(query_offset[j] + b);
             c.q_count = (int)std::min<long long>(chunk_q, query_count[j] - b);
             c.pad = 0;
@@ -333,10 +346,9 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     std::vector<int> tpis(chunks.size());
     for (size_t i = 0; i < order.size(); ++i) {
         sorted[i] = chunks[order[i]];
-        tpis[i] = tpi_for_width(models[sorted[i].model]->hdr.max_width);
+        tpis[i] = tpi_for_width(models[used[sorted[i].model]]->hdr.max_width);
     }
-    std::vector<NiqModelRef> refs(n_models);
-    for (int i = 0; i < n_models; ++i) refs[i] = models[i] ? models[i]->ref() : NiqModelRef{nullptr, nullptr};
+    const int n_refs = (int)refs.size();
     const size_t n_chunks = sorted.size();
     char* b = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
     size_t off = 0;
@@ -348,7 +360,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     int* d_tpi = reinterpret_cast<int*>(b + off);
     off += al(std::max<size_t>(n_chunks, 1) * 4);
     NiqModelRef* d_models = reinterpret_cast<NiqModelRef*>(b + off);
-    off += al((size_t)n_models * sizeof(NiqModelRef));
+    off += al((size_t)n_refs * sizeof(NiqModelRef));
     float* stacks = reinterpret_cast<float*>(b + off);
     NIQ_REQUIRE(off + slots_max() * kBStack * 24 <= workspace_bytes - 256, NIQ_ERR_CAPACITY, "workspace too small");
     NIQ_CUDA(cudaMemsetAsync(b, 0, 64, s));
@@ -357,7 +369,7 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     // host staging: these copies are synchronous w.r.t. the host buffers (pageable memory)
     NIQ_CUDA(cudaMemcpyAsync(d_chunks, sorted.data(), n_chunks * sizeof(BChunk), cudaMemcpyHostToDevice, s));
     NIQ_CUDA(cudaMemcpyAsync(d_tpi, tpis.data(), n_chunks * 4, cudaMemcpyHostToDevice, s));
-    NIQ_CUDA(cudaMemcpyAsync(d_models, refs.data(), n_models * sizeof(NiqModelRef), cudaMemcpyHostToDevice, s));
+    NIQ_CUDA(cudaMemcpyAsync(d_models, refs.data(), n_refs * sizeof(NiqModelRef), cudaMemcpyHostToDevice, s));
     BArgs a;
     a.models = d_models;
     a.chunks = d_chunks;

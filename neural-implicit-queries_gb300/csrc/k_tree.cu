@@ -125,12 +125,13 @@ __global__ void __launch_bounds__(kNT) k_tree(NiqModelRef M, TreeParams P, TreeW
                         const float mid = d == 0 ? __fmul_rn(0.5f, __fadd_rn(l0, h0))
                                         : d == 1 ? __fmul_rn(0.5f, __fadd_rn(l1, h1))
                                                  : __fmul_rn(0.5f, __fadd_rn(l2, h2));
-                        const float alo[3] = {l0, l1, l2};
-                        const float ahi[3] = {d == 0 ? mid : h0, d == 1 ? mid : h1, d == 2 ? mid : h2};
-                        const float blo[3] = {d == 0 ? mid : l0, d == 1 ? mid : l1, d == 2 ? mid : l2};
-                        const float bhi[3] = {h0, h1, h2};
-                        put_node(out_lo, out_hi, pc, alo, ahi);
-                        put_node(out_lo, out_hi, pc + 1, blo, bhi);
+                        // child A = [lo, hi with hi[d] = mid], child B = [lo with lo[d] = mid, hi]
+                        float* ol = out_lo + 3 * pc;
+                        float* oh = out_hi + 3 * pc;
+                        ol[0] = l0; ol[1] = l1; ol[2] = l2;
+                        oh[0] = d == 0 ? mid : h0; oh[1] = d == 1 ? mid : h1; oh[2] = d == 2 ? mid : h2;
+                        ol[3] = d == 0 ? mid : l0; ol[4] = d == 1 ? mid : l1; ol[5] = d == 2 ? mid : l2;
+                        oh[3] = h0; oh[4] = h1; oh[5] = h2;
                     } else {
                         niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
                     }

@@ -332,6 +332,22 @@ def test_batched_results_independent_of_tuning(niq, gpu_ready):
         at.set_params(**old)
 
 
+def test_batched_jobs_over_a_subset_of_a_large_table(niq, gpu_ready):
+    """Jobs that use a few models of a large table (as the autotuner's sample does) fit the
+    workspace sized by the job count, and return the same distances as the table of just
+    those models."""
+    models = [niq.workloads.he_mlp([3, 32, 32, 1], 'relu', seed=60 + i, grid=8) for i in range(40)]
+    table = niq.batched.ModelTable(models)
+    f = gf(niq, models[0], conservative=True)
+    rng = np.random.default_rng(12)
+    qs = [rng.uniform(-1.2, 1.2, (n, 3)).astype(np.float32) for n in (50, 80, 30)]
+    lo, hi = -np.ones(3, np.float32), np.ones(3, np.float32)
+    big = niq.batched.closest_point_many(f, table, [37, 5, 37], qs, lo, hi, 1e-2)
+    small = niq.batched.closest_point_many(f, [models[37], models[5]], [0, 1, 0], qs, lo, hi, 1e-2)
+    for (d_big, _), (d_small, _) in zip(big, small):
+        np.testing.assert_array_equal(d_big, d_small)
+
+
 @pytest.mark.parametrize('B', [2048, 100])
 def test_tree_schedules_agree(niq, gpu_ready, B):
     """The persistent tree, one launch per level, and the reference's schedule (launches
