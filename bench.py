@@ -294,25 +294,25 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-# DRAM bytes per classified box of the tree kernels (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch on the 24-bisection tree of the 12-sphere model,
-# divided by its boxes): the level arrays stay in L2, so a box costs well under its 24 B
-# of node I/O.  Keyed by the engine code of niq_tree_engine.
-TREE_DRAM_BYTES_PER_BOX = {0: (148480 + 6912) / 332953}
-TREE_DRAM_SOURCE = {0: "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tree on the 18-bisection tree "
-                       "(155.4 KB for 332,953 boxes), scaled by boxes"}
+# DRAM bytes per classified box of the tree kernels: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one k_tree launch on this workload (24 bisections, the timed
+# step after the L2 flush): 0.48 MB read, 16.67 MB written -- the 727,581 unknown leaves
+# of 24 B; the level arrays stay in L2.  Keyed by the engine code of niq_tree_engine.
+TREE_DRAM_BYTES_PER_BOX = {0: (475392 + 16673536) / 3735843}
+TREE_DRAM_SOURCE = {0: "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_tree launch on the 24-bisection "
+                       "tree (0.48 MB read, 16.67 MB written for 3,735,843 boxes: the leaf output)"}
 
 
 def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
     """Roofline of the tree kernel: algorithmic FLOPs (2 (v + 2) S per box) over the
     tree phase's CUDA-event time.  The FP32 engine is bound by the FP32 FMA pipe; the
     tensor-core engine executes the four signed rows of every hidden layer as 3 tf32
-    products per FLOP on the tensor pipe (dense tf32 peak = half the measured bf16 burst)
+    products per FLOP on the tensor pipe (tf32 ceiling measured live, tf32_peak_tflops)
     and the err row and the linearisations on the FP32 pipe, so both fractions are given."""
     hidden = sum(A.shape[0] * A.shape[1] for A, _, _ in importlib.import_module(PKG).mlp.spec_layers(params)[1:-1])
     achieved = n_boxes * bf / t_tree / 1e12
     fp32_peak = fp32_peak_tflops(device)
-    tf32_peak = measured_peaks().get('bf16_tflops', 1900.) / 2
+    tf32_peak = tf32_peak_tflops() if engine == 1 else None
     per_box = TREE_DRAM_BYTES_PER_BOX.get(engine)
     out = {"kernel": "k_tree_tc (persistent level-set tree, tensor cores)" if engine == 1
            else "k_tree (persistent level-set tree)",
@@ -324,8 +324,8 @@ def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
         out.update({"bound": "tensor", "peak": tf32_peak, "frac": achieved / tf32_peak,
                     "tensor_pipe_tflops": tensor, "tensor_pipe_frac": tensor / tf32_peak,
                     "fp32_peak": fp32_peak, "frac_of_fp32_peak": achieved / fp32_peak,
-                    "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json); FP32 FMA "
-                                   "pipe: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock"})
+                    "peak_source": TF32_PEAK_SOURCE + "; FP32 FMA pipe: SMs x 128 lanes x 2 FLOP x the "
+                                   "measured maximum SM clock"})
     else:
         out.update({"bound": "fp32", "peak": fp32_peak, "frac": achieved / fp32_peak,
                     "peak_source": "FP32 FMA pipe: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock "
@@ -447,11 +447,10 @@ def precision_sample(niq, steps, warmup):
         out[name] = {"boxes_per_s": nb / tb, "classify_ms": tb * 1e3, "rays_per_s": rs.shape[0] / tr,
                      "cast_ms": tr * 1e3, "ray_steps": int(r[2].sum().item()),
                      "achieved_tflops": nb * fl / tb / 1e12}
-    tf32_peak = measured_peaks().get('bf16_tflops', 1900.) / 2
+    tf32_peak = tf32_peak_tflops()
     a3 = 3 * out["3xtf32"]["achieved_tflops"]
     out["3xtf32"]["roofline"] = {"bound": "tensor", "achieved": a3, "peak": tf32_peak, "unit": "TFLOP/s",
-                                 "frac": a3 / tf32_peak,
-                                 "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json)"}
+                                 "frac": a3 / tf32_peak, "peak_source": TF32_PEAK_SOURCE}
     out["tensor_vs_fp32"] = {"boxes": out["3xtf32"]["boxes_per_s"] / out["fp32"]["boxes_per_s"],
                              "rays": out["3xtf32"]["rays_per_s"] / out["fp32"]["rays_per_s"]}
     out["config"] = {"workload": "precision_relu256x8_truncate256", "boxes": nb, "rays": int(rs.shape[0]),
@@ -598,6 +597,20 @@ def measured_peaks():
         return {}
 
 
+def tf32_peak_tflops():
+    """The tensor-core ceiling of the 3xTF32 engine's dense step, measured live on this GPU
+    (niq_tc_tf32_rate: the engine's own MMA sequence, no staging or epilogue)."""
+    lib = importlib.import_module(PKG + '._lib')
+    L = lib.load()
+    v = lib.C.c_float(0.)
+    lib.check(L.niq_tc_tf32_rate(4096, lib.C.byref(v), None))
+    return float(v.value)
+
+
+TF32_PEAK_SOURCE = ("tcgen05 kind::tf32 rate of the engine's dense step measured live on this GPU "
+                    "(niq_tc_tf32_rate); MEASURED_PEAKS.json has no tf32 figure")
+
+
 def fp32_peak_tflops(device=0):
     """FP32 FMA pipe peak: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock."""
     import torch
@@ -654,8 +667,7 @@ def run_precision(args):
     c = torch.from_numpy(rng.uniform(-0.8, 0.8, (nb, 3)).astype(np.float32)).cuda()
     vv = torch.from_numpy(np.tile((0.01 * np.eye(3, dtype=np.float32))[None], (nb, 1, 1))).cuda()
     peak32 = fp32_peak_tflops(torch.cuda.current_device())
-    peaks = measured_peaks()
-    tf32_peak = peaks.get('bf16_tflops', 1900.) / 2
+    tf32_peak = tf32_peak_tflops()
     forms = [("affine_fixed", 'affine_fixed', {}, 'auto', box_flop(3)),
              ("affine_truncate256_fp32", 'affine_truncate', {'affine_n_truncate': 256}, 'fp32', box_flop(3, 256)),
              ("affine_truncate256_3xtf32", 'affine_truncate', {'affine_n_truncate': 256}, '3xtf32', box_flop(3, 256))]
@@ -681,8 +693,7 @@ def run_precision(args):
         if products == '3xtf32':
             row["tensor_tflops"] = 3 * tf
             row["roofline"] = {"bound": "tensor", "achieved": 3 * tf, "peak": tf32_peak, "unit": "TFLOP/s",
-                               "frac": 3 * tf / tf32_peak,
-                               "peak_source": "dense tf32 = half the measured bf16 burst (MEASURED_PEAKS.json)"}
+                               "frac": 3 * tf / tf32_peak, "peak_source": TF32_PEAK_SOURCE}
         else:
             row["roofline"] = {"bound": "fp32", "achieved": tf, "peak": peak32, "unit": "TFLOP/s", "frac": tf / peak32}
         out[name] = row

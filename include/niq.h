@@ -121,6 +121,13 @@ int niq_tune_set(int32_t param, int32_t value);
 int niq_tune_get(int32_t param, int32_t* value);
 /* Number of SMs and resident-CTA counts of the current device (for workspace sizing). */
 int niq_device_info(int32_t* sm_count, int32_t* max_smem_per_block);
+/* The tensor-core ceiling of the 3xTF32 engine on the current device (no counterpart in
+ * the reference: it calibrates the roofline of the tensor-core kernels).  One CTA per SM
+ * issues, per 16-deep chunk, the engine's dense step -- the three split products of two
+ * M = 128 tiles at N = 256 from its three-stage shared-memory ring -- for `chunks` chunks
+ * with no staging and no epilogue; *tflops_out receives the measured rate in tf32
+ * TFLOP/s.  Synchronises `stream`; allocates no device memory. */
+int niq_tc_tf32_rate(int32_t chunks, float* tflops_out, void* stream);
 
 /* ---- models: the dict spec of src/mlp.py:14-24,117-144 packed by the host layer ---- */
 /* Validates and uploads a packed spec (host memory) to the current device.
@@ -192,9 +199,15 @@ typedef struct niq_frustum_camera {
  * are (res_x, res_y) arrays indexed [x][y] as the reference returns them: t_out, hit_id
  * (1-based function index, 0 = none) and count (steps per pixel, truncated);
  * n_evals_out (device int64) counts frustum steps.  One launch per iteration with a
- * host read of the live count, as the reference's loop.  Modes: interval, affine_fixed,
- * slope_interval.  workspace: niq_cast_frustum_workspace_size() bytes. */
+ * host read of the live count, as the reference's loop.  Every mode: interval,
+ * affine_fixed and slope_interval in one fused kernel per iteration (workspace:
+ * niq_cast_frustum_workspace_size() bytes); affine_truncate, affine_all and
+ * affine_append bound each substep's boxes with the growing-term engine between
+ * per-frustum kernels (workspace: niq_cast_frustum_growing_workspace_size() bytes). */
 size_t niq_cast_frustum_workspace_size(int32_t res_x, int32_t res_y, int32_t n_side_init);
+size_t niq_cast_frustum_growing_workspace_size(const niq_model* const* models, int32_t nfunc,
+                                               const niq_bound_opts* opts, int32_t res_x, int32_t res_y,
+                                               int32_t n_side_init);
 int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bound_opts* opts,
                      const niq_frustum_camera* camera, const niq_cast_opts* cast, float refine_width_fac,
                      int32_t n_side_init, float* t_out, int32_t* hit_id_out, int32_t* count_out,

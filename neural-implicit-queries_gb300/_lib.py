@@ -79,6 +79,7 @@ _SIGS = {
     'niq_last_error': (C.c_char_p, []),
     'niq_version': (C.c_int, []),
     'niq_device_info': (C.c_int, [C.POINTER(_I32), C.POINTER(_I32)]),
+    'niq_tc_tf32_rate': (C.c_int, [_I32, _PF, _P]),
     'niq_tune_set': (C.c_int, [_I32, _I32]),
     'niq_tune_get': (C.c_int, [_I32, C.POINTER(_I32)]),
     'niq_model_create': (C.c_int, [_P, _SZ, C.POINTER(_P)]),
@@ -96,6 +97,7 @@ _SIGS = {
     'niq_tree_workspace_size': (_SZ, [_I64, _I32]),
     'niq_levelset_tree': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I32, _I64, _F32, _I32, _I64, _P, _P, _SZ, _P]),
     'niq_cast_frustum_workspace_size': (_SZ, [_I32, _I32, _I32]),
+    'niq_cast_frustum_growing_workspace_size': (_SZ, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I32, _I32, _I32]),
     'niq_cast_frustum': (C.c_int, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), C.POINTER(FrustumCamera),
                                    C.POINTER(CastOpts), _F32, _I32, _P, _P, _P, _P, _P, _SZ, _P]),
     'niq_sample_workspace_size': (_SZ, [_I64]),

@@ -18,7 +18,9 @@
 // forward pass for 'interval' and 'affine_fixed' (8 rows: center, three vectors, two
 // points, err); 'slope_interval' uses a bound pass and a point pass.
 #include <cmath>
+#include <vector>
 #include "cast_common.cuh"
+#include "wide_engine.cuh"
 
 namespace niq {
 
@@ -292,6 +294,173 @@ __global__ void __launch_bounds__(kNT) k_frust(ModelSet S, int mode_interval, Fr
     if (threadIdx.x < S.n && s_evals[threadIdx.x]) atomicAdd(&n_evals[threadIdx.x], s_evals[threadIdx.x]);
 }
 
+// ---------------------------------------------------------------- growing-term modes
+// 'affine_truncate', 'affine_all', 'affine_append': each substep's boxes are bounded by
+// the growing-term engine (wide_classify, v = 3) and the hit-test points by the point
+// kernel, between per-frustum kernels that hold k_frust's arithmetic op by op.
+struct WFrust {
+    float* geo;    // per live frustum: mid[3], d1[3], d2[3], expand (10 floats)
+    int* single;   // single-pixel frustum
+    int* hit;      // hit flag, hit id, steps taken, demands subdivision
+    int* hitid;
+    int* steps;
+    int* demand;
+    float* center; // (n, 3) box centers
+    float* vecs;   // (n, 3, 3): along the central ray, across, up
+    float* pts;    // (n, 2, 3): the two hit-test points
+    int* sign;     // (nfunc, n)
+    float* vals;   // (nfunc, n, 2)
+};
+
+// Frustum geometry (src/queries.py:272-306) of every live frustum, state cleared.
+__global__ void k_wfr_setup(FrustCam cam, FrustList in, long long n_live, WFrust W) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_live; i += (long long)gridDim.x * blockDim.x) {
+        const int4 rg = in.rng[i];
+        W.single[i] = (rg.x + 1 == rg.z) && (rg.y + 1 == rg.w);
+        const float xl = __fsub_rn(__fdiv_rn(__fmul_rn(2.f, (float)rg.x), cam.rx1), 1.f);
+        const float xu = __fsub_rn(__fdiv_rn(__fmul_rn(2.f, (float)(rg.z - 1)), cam.rx1), 1.f);
+        const float yl = __fsub_rn(__fdiv_rn(__fmul_rn(2.f, (float)rg.y), cam.ry1), 1.f);
+        const float yu = __fsub_rn(__fdiv_rn(__fmul_rn(2.f, (float)(rg.w - 1)), cam.ry1), 1.f);
+        float uu[3], lu[3], ul[3], ll[3];
+        frust_ray(cam, xu, yu, uu);
+        frust_ray(cam, xl, yu, lu);
+        frust_ray(cam, xu, yl, ul);
+        frust_ray(cam, xl, yl, ll);
+        float m[3];
+        for (int k = 0; k < 3; ++k) m[k] = __fmul_rn(0.5f, __fadd_rn(uu[k], ll[k]));
+        const float ml = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], m[0]), __fmul_rn(m[1], m[1])), __fmul_rn(m[2], m[2])));
+        float* g = W.geo + 10 * i;
+        for (int k = 0; k < 3; ++k) {
+            g[k] = __fdiv_rn(m[k], ml);
+            g[3 + k] = __fsub_rn(uu[k], lu[k]);
+            g[6 + k] = __fsub_rn(uu[k], ul[k]);
+        }
+        g[9] = __fdiv_rn(1.f, ml);
+        W.hit[i] = 0;
+        W.hitid[i] = 0;
+        W.steps[i] = 0;
+        W.demand[i] = 0;
+    }
+}
+
+// One substep's boxes and hit-test points (src/queries.py:206-244).
+__global__ void k_wfr_prep(FrustCam cam, CastDev o, FrustList in, long long n_live, WFrust W) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_live; i += (long long)gridDim.x * blockDim.x) {
+        const float* g = W.geo + 10 * i;
+        const float t = in.t[i], sz = in.size[i];
+        const float tadj = __fmul_rn(__fadd_rn(t, sz), g[9]);
+        for (int k = 0; k < 3; ++k) {
+            const float mk = g[k], rt = cam.root[k];
+            const float rfr = __fdiv_rn(__fmul_rn(g[3 + k], tadj), 2.f);
+            const float ufr = __fdiv_rn(__fmul_rn(g[6 + k], tadj), 2.f);
+            const float cen = __fadd_rn(rt, __fmul_rn(__fmul_rn(0.5f, __fadd_rn(t, tadj)), mk));
+            const float cv = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(tadj, t)), mk);
+            W.center[3 * i + k] = cen;
+            W.vecs[9 * i + k] = cv;
+            W.vecs[9 * i + 3 + k] = rfr;
+            W.vecs[9 * i + 6 + k] = ufr;
+            W.pts[6 * i + k] = __fadd_rn(rt, __fmul_rn(t, mk));
+            W.pts[6 * i + 3 + k] = __fadd_rn(rt, __fmul_rn(__fadd_rn(t, o.hit_eps), mk));
+        }
+    }
+}
+
+// The substep's decisions from the signs and point values, then the step rule
+// (src/queries.py:245-267), as k_frust takes them.
+__global__ void k_wfr_update(CastDev o, FrustList in, long long n_live, int nfunc, WFrust W) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_live; i += (long long)gridDim.x * blockDim.x) {
+        const bool hit_before = W.hit[i] != 0;
+        bool can = !hit_before;
+        bool hit = hit_before;
+        int hid = W.hitid[i];
+        if (!hit_before) {
+            W.steps[i] += 1;
+            for (int f = 0; f < nfunc; ++f) {
+                if (W.sign[(long long)f * n_live + i] == NIQ_SIGN_UNKNOWN) can = false;
+                const float v0 = W.vals[((long long)f * n_live + i) * 2], v1 = W.vals[((long long)f * n_live + i) * 2 + 1];
+                const int sg0 = (v0 > 0.f) - (v0 < 0.f), sg1 = (v1 > 0.f) - (v1 < 0.f);
+                if ((v0 != v0) || (v1 != v1) || sg0 != sg1) { hid = f + 1; hit = true; }
+            }
+        }
+        const float sz = in.size[i];
+        const float this_step = can ? sz : __fmul_rn(o.hit_eps, W.single[i] ? 1.f : 0.f);
+        if (!hit) in.t[i] = __fadd_rn(in.t[i], __fmul_rn(this_step, o.safety));
+        const float ns = can ? __fmul_rn(sz, o.grow) : __fmul_rn(sz, o.shrink);
+        if (ns < o.hit_eps || hit) W.demand[i] = 1;
+        in.size[i] = fmaxf(ns, o.hit_eps);
+        W.hit[i] = hit;
+        W.hitid[i] = hid;
+    }
+}
+
+// Count, termination, refinement and the appends of one iteration (src/queries.py:323-467),
+// as the tail of k_frust.  Every lane of a warp joins the warp-aggregated reservations.
+__global__ void k_wfr_finish(FrustCam cam, CastDev o, float refine_fac, int iter, FrustList in, long long n_live,
+                             FrustList out, FrustList fin, int* __restrict__ fin_hit, FrustWs* ws, long long cap,
+                             WFrust W) {
+    for (long long i0 = blockIdx.x * (long long)blockDim.x; i0 < n_live; i0 += (long long)gridDim.x * blockDim.x) {
+        const long long i = i0 + threadIdx.x;
+        bool term = false, refine = false;
+        int4 rg = make_int4(0, 0, 0, 0);
+        float cnt = 0.f, t = 0.f, sz = 0.f;
+        if (i < n_live) {
+            rg = in.rng[i];
+            t = in.t[i];
+            sz = in.size[i];
+            const int area = (rg.z - rg.x) * (rg.w - rg.y);
+            cnt = __fadd_rn(in.count[i], __fmul_rn((float)W.steps[i], __fdiv_rn(1.f, (float)area)));
+            const bool hit = W.hit[i] && area == 1;
+            term = hit || (t > o.max_dist) || (iter >= o.n_max_step);
+            if (!term) {
+                const float wx = __fmul_rn(__fmul_rn(2.f, sinf(__fdiv_rn(__fmul_rn(cam.half_x, (float)(rg.z - rg.x)), (float)cam.res_x))), t);
+                const float wy = __fmul_rn(__fmul_rn(2.f, sinf(__fdiv_rn(__fmul_rn(cam.half_y, (float)(rg.w - rg.y)), (float)cam.res_y))), t);
+                const bool can_subd = (rg.z > rg.x + 1) || (rg.w > rg.y + 1);
+                const float lim = __fmul_rn(refine_fac, sz);
+                refine = can_subd && (wx > lim || wy > lim || W.demand[i]);
+            }
+        }
+        const bool keep = i < n_live && !term && !refine;
+        const long long pf = niq_warp_reserve(&ws->n_fin, term, 1);
+        const long long pk = niq_warp_reserve(&ws->n_next, keep, 1);
+        const long long pr = niq_warp_reserve(&ws->n_next, refine, 2);
+        if (term) {
+            if (pf < cap) {
+                fin.rng[pf] = rg;
+                fin.t[pf] = t;
+                fin.count[pf] = cnt;
+                fin_hit[pf] = W.hitid[i];
+            } else {
+                niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+            }
+        }
+        if (keep) {
+            if (pk < cap) {
+                out.rng[pk] = rg;
+                out.t[pk] = t;
+                out.size[pk] = sz;
+                out.count[pk] = cnt;
+            } else {
+                niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+            }
+        }
+        if (refine) {
+            if (pr + 1 < cap) {
+                const bool sx = (rg.z - rg.x) >= (rg.w - rg.y);
+                const int xm = (rg.x + rg.z) / 2, ym = (rg.y + rg.w) / 2;
+                out.rng[pr] = make_int4(rg.x, rg.y, sx ? xm : rg.z, sx ? rg.w : ym);
+                out.rng[pr + 1] = make_int4(sx ? xm : rg.x, sx ? rg.y : ym, rg.z, rg.w);
+                for (int q = 0; q < 2; ++q) {
+                    out.t[pr + q] = t;
+                    out.size[pr + q] = sz;
+                    out.count[pr + q] = cnt;
+                }
+            } else {
+                niq_flag_error(&ws->err, NIQ_ERR_CAPACITY);
+            }
+        }
+    }
+}
+
 // Initial frusta: an n_side x n_side grid of pixel tiles (src/queries.py:506-517).
 __global__ void k_frust_init(FrustList L, const int* xt, const int* yt, int ns, float init_size) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -357,11 +526,58 @@ static FrustList frust_list(char* base, size_t off, long long cap) {
     return L;
 }
 
+// Extra workspace of the growing-term path: the per-frustum state and step buffers of up
+// to `cap` live frusta, then the growing-term engine's own slots (the largest over the
+// functions).
+struct WFrustLayout {
+    size_t geo, single, hit, hitid, steps, demand, center, vecs, pts, sign, vals, wide, total;
+};
+
+static WFrustLayout wfr_layout(const niq_model* const* models, int nfunc, const niq_bound_opts& o, long long cap,
+                               size_t base) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    WFrustLayout W;
+    const size_t n = (size_t)cap;
+    W.geo = base;
+    W.single = W.geo + al(40 * n);
+    W.hit = W.single + al(4 * n);
+    W.hitid = W.hit + al(4 * n);
+    W.steps = W.hitid + al(4 * n);
+    W.demand = W.steps + al(4 * n);
+    W.center = W.demand + al(4 * n);
+    W.vecs = W.center + al(12 * n);
+    W.pts = W.vecs + al(36 * n);
+    W.sign = W.pts + al(24 * n);
+    W.vals = W.sign + al(4 * n * (size_t)nfunc);
+    W.wide = W.vals + al(8 * n * (size_t)nfunc);
+    size_t wmax = 0;
+    for (int f = 0; f < nfunc; ++f)
+        if (models && models[f]) {
+            const size_t b = wide_workspace_bytes(models[f]->hdr, o, 3);
+            wmax = wmax > b ? wmax : b;
+        }
+    W.total = W.wide + al(wmax) + 256;
+    return W;
+}
+
+static int wfr_grid(long long n) {
+    const long long g = (n + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
 }  // namespace niq
 
 using namespace niq;
 
 extern "C" {
+
+size_t niq_cast_frustum_growing_workspace_size(const niq_model* const* models, int32_t nfunc,
+                                               const niq_bound_opts* opts, int32_t res_x, int32_t res_y,
+                                               int32_t n_side_init) {
+    if (!models || !opts || nfunc < 1 || nfunc > kMaxFuncs || res_x < 1 || res_y < 1 || n_side_init < 1) return 0;
+    const FrustLayout FL = frust_layout(res_x, res_y, n_side_init);
+    return wfr_layout(models, nfunc, *opts, FL.cap, FL.total).total;
+}
 
 size_t niq_cast_frustum_workspace_size(int32_t res_x, int32_t res_y, int32_t n_side_init) {
     if (res_x < 1 || res_y < 1 || n_side_init < 1) return 0;
@@ -375,8 +591,9 @@ int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bo
     NIQ_REQUIRE(opts && camera && cast && t_out && hit_id_out && count_out && n_evals_out, NIQ_ERR_INVALID_ARG,
                 "null argument");
     const int mode = opts->mode;
-    NIQ_REQUIRE(mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
-                NIQ_ERR_UNSUPPORTED, "the frustum cast supports the interval, affine_fixed and slope_interval modes");
+    const bool growing = mode == NIQ_MODE_AFFINE_TRUNCATE || mode == NIQ_MODE_AFFINE_ALL || mode == NIQ_MODE_AFFINE_APPEND;
+    NIQ_REQUIRE(growing || mode == NIQ_MODE_AFFINE_FIXED || mode == NIQ_MODE_INTERVAL || mode == NIQ_MODE_SLOPE_INTERVAL,
+                NIQ_ERR_UNSUPPORTED, "unknown bound mode %d", mode);
     const int rx = camera->res_x, ry = camera->res_y, ns = n_side_init;
     NIQ_REQUIRE(rx >= 1 && ry >= 1 && (long long)rx * ry < (1ll << 31), NIQ_ERR_INVALID_ARG, "bad resolution");
     NIQ_REQUIRE(ns >= 1 && ns <= rx && ns <= ry, NIQ_ERR_INVALID_ARG, "n_side_init must be in [1, min(res_x, res_y)]");
@@ -386,7 +603,8 @@ int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bo
     int rc = make_set(models, nfunc, S, maxw, wfloats, maxlayer);
     if (rc) return rc;
     const FrustLayout FL = frust_layout(rx, ry, ns);
-    NIQ_REQUIRE(workspace && workspace_bytes >= FL.total, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", FL.total);
+    const size_t need = growing ? wfr_layout(models, nfunc, *opts, FL.cap, FL.total).total : FL.total;
+    NIQ_REQUIRE(workspace && workspace_bytes >= need, NIQ_ERR_CAPACITY, "workspace of %zu bytes needed", need);
     cudaStream_t s = as_stream(stream);
     char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
     FrustWs* ws = reinterpret_cast<FrustWs*>(base + FL.hdr);
@@ -471,8 +689,64 @@ int niq_cast_frustum(const niq_model* const* models, int32_t nfunc, const niq_bo
         }
         return NIQ_OK;
     };
+    // the growing-term modes: per iteration the geometry, then per substep the boxes and
+    // points, the growing-term engine and the point kernel per function, the step rule;
+    // then the iteration's appends -- one host read of the live count per iteration
+    auto run_growing = [&]() -> int {
+        const WFrustLayout WL = wfr_layout(models, nfunc, *opts, FL.cap, FL.total);
+        WFrust W;
+        W.geo = reinterpret_cast<float*>(base + WL.geo);
+        W.single = reinterpret_cast<int*>(base + WL.single);
+        W.hit = reinterpret_cast<int*>(base + WL.hit);
+        W.hitid = reinterpret_cast<int*>(base + WL.hitid);
+        W.steps = reinterpret_cast<int*>(base + WL.steps);
+        W.demand = reinterpret_cast<int*>(base + WL.demand);
+        W.center = reinterpret_cast<float*>(base + WL.center);
+        W.vecs = reinterpret_cast<float*>(base + WL.vecs);
+        W.pts = reinterpret_cast<float*>(base + WL.pts);
+        W.sign = reinterpret_cast<int*>(base + WL.sign);
+        W.vals = reinterpret_cast<float*>(base + WL.vals);
+        void* wws = base + WL.wide;
+        const size_t wws_bytes = workspace_bytes - (size_t)(base - reinterpret_cast<char*>(workspace)) - WL.wide;
+        long long n_live = (long long)ns * ns;
+        int cur = 0, it = 0;
+        while (n_live > 0) {
+            NIQ_CUDA(cudaMemsetAsync(&ws->n_next, 0, sizeof(unsigned long long), s));
+            const int blocks = wfr_grid(n_live);
+            k_wfr_setup<<<blocks, 256, 0, s>>>(cam, lists[cur], n_live, W);
+            NIQ_CUDA(cudaGetLastError());
+            for (int sub = 0; sub < cd.n_substeps; ++sub) {
+                k_wfr_prep<<<blocks, 256, 0, s>>>(cam, cd, lists[cur], n_live, W);
+                NIQ_CUDA(cudaGetLastError());
+                for (int f = 0; f < nfunc; ++f) {
+                    int r2 = wide_classify(models[f], *opts, n_live, W.center, W.vecs, 3, 0.f,
+                                           W.sign + (long long)f * n_live, nullptr, wws, wws_bytes, s);
+                    if (r2) return r2;
+                    r2 = niq_eval_points(models[f], 2 * n_live, W.pts, W.vals + (long long)f * 2 * n_live, s);
+                    if (r2) return r2;
+                }
+                k_wfr_update<<<blocks, 256, 0, s>>>(cd, lists[cur], n_live, nfunc, W);
+                NIQ_CUDA(cudaGetLastError());
+            }
+            k_wfr_finish<<<blocks, 256, 0, s>>>(cam, cd, refine_width_fac, it, lists[cur], n_live, lists[1 - cur], fin,
+                                                fin_hit, ws, FL.cap, W);
+            NIQ_CUDA(cudaGetLastError());
+            steps_total += n_live;
+            unsigned long long next = 0;
+            int err = 0;
+            NIQ_CUDA(cudaMemcpyAsync(&next, &ws->n_next, sizeof(next), cudaMemcpyDeviceToHost, s));
+            NIQ_CUDA(cudaMemcpyAsync(&err, &ws->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+            NIQ_CUDA(cudaStreamSynchronize(s));
+            NIQ_REQUIRE(err == 0, err, "frustum kernel error %d", err);
+            n_live = (long long)next;
+            it += cast->n_substeps;
+            cur = 1 - cur;
+        }
+        return NIQ_OK;
+    };
 #define NIQ_FRUST(CC, SL) NIQ_DISPATCH_TPI(tpi, { rc = run(k_frust<TPI, CC, SL>, TPI); })
-    if (slope) { if (cons) { NIQ_FRUST(true, true); } else { NIQ_FRUST(false, true); } }
+    if (growing) { rc = run_growing(); }
+    else if (slope) { if (cons) { NIQ_FRUST(true, true); } else { NIQ_FRUST(false, true); } }
     else { if (cons) { NIQ_FRUST(true, false); } else { NIQ_FRUST(false, false); } }
 #undef NIQ_FRUST
     if (rc) return rc;

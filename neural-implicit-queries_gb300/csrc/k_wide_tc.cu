@@ -717,6 +717,83 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     }
 }
 
+// ---------------------------------------------------------------- roofline calibration
+// The dense step alone: per 16-deep chunk, the three split products of two M = 128 tiles
+// at N = 256 from the three-stage ring, exactly as k_wide_tc issues them, with no
+// staging and no epilogue.  One CTA per SM; the rate is the tensor pipe's tf32 ceiling
+// for this instruction sequence on this GPU.
+__device__ int g_tc_rate_status;
+
+__global__ void __launch_bounds__(kTcNT, 1) k_tc_rate(int chunks, long long polls) {
+    extern __shared__ __align__(1024) float smem[];
+    __shared__ __align__(8) uint64_t bar[kTcStages];
+    __shared__ uint32_t s_tmem;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < kTcStages * kTcStage; i += kTcNT) smem[i] = 1e-3f * (float)(i & 7);
+    if (warp == 0) tc::tmem_alloc(&s_tmem, 512);
+    if (tid == 0) {
+        for (int i = 0; i < kTcStages; ++i) tc::mbar_init(&bar[i], 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = s_tmem;
+    if (tid == 0) {
+        const uint32_t idesc = tc::idesc_tf32(128, 256);
+        const uint32_t sbo = (kTcKC / 4) * 128;
+        uint32_t phase = 0u;
+        bool ok = true;
+        int issued = 0, waited = 0;   // commits made, commits waited for (in order)
+        for (int c = 0; c < chunks && ok; ++c) {
+            const int s = c % kTcStages;
+            if (c >= kTcStages) {   // the stage's previous MMAs, as before a restage
+                ok = tc::mbar_wait(&bar[s], (phase >> s) & 1u, polls);
+                if (!ok) break;
+                phase ^= 1u << s;
+                ++waited;
+            }
+            const uint32_t xh = tc::smem_addr(smem + s * kTcStage), xl = xh + kTcRows * kTcKC * 4;
+            const uint32_t wh = xh + 2 * kTcRows * kTcKC * 4, wl = xh + 3 * kTcRows * kTcKC * 4;
+#pragma unroll
+            for (int ks = 0; ks < kTcKC / 8; ++ks) {
+                const uint64_t bh = tc::smem_desc(wh + ks * 256, 128, sbo);
+                const uint64_t bl = tc::smem_desc(wl + ks * 256, 128, sbo);
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const uint32_t toff = (uint32_t)t * 128 / 8 * sbo + ks * 256;
+                    const uint64_t ah = tc::smem_desc(xh + toff, 128, sbo);
+                    const uint64_t al = tc::smem_desc(xl + toff, 128, sbo);
+                    const uint32_t d = tmem + (uint32_t)(t * 256);
+                    tc::mma_tf32(d, ah, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                    tc::mma_tf32(d, ah, bl, idesc, 1u);
+                    tc::mma_tf32(d, al, bh, idesc, 1u);
+                }
+            }
+            tc::mma_commit(&bar[s]);
+            ++issued;
+        }
+        // the commits not yet waited for, in order; with the built-in limit after a
+        // give-up, so no MMA is in flight when the tensor memory is released
+        for (; waited < issued; ++waited) {
+            const int s = waited % kTcStages;
+            if (!tc::mbar_wait(&bar[s], (phase >> s) & 1u, ok ? polls : kMbarPollsDefault)) {
+                ok = false;
+                if (!tc::mbar_wait(&bar[s], (phase >> s) & 1u, kMbarPollsDefault)) break;
+            }
+            phase ^= 1u << s;
+        }
+        if (!ok) atomicExch(&g_tc_rate_status, NIQ_ERR_TIMEOUT);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tmem_relinquish();
+        tc::tmem_dealloc(tmem, 512);
+    }
+}
+
 // Split transposed weights: for a layer, hi then lo, each [chunk][o16 rows][16] in the
 // K-major core-matrix layout; zero beyond the layer's in/out.
 __global__ void k_tc_split_weights(NiqModelRef M, int li, float* dst) {
@@ -828,3 +905,36 @@ int wide_tc_classify(const niq_model* m, const niq_bound_opts& o, long long n, c
 }
 
 }  // namespace niq
+
+using namespace niq;
+
+extern "C" int niq_tc_tf32_rate(int32_t chunks, float* tflops_out, void* stream) {
+    NIQ_REQUIRE(tflops_out && chunks >= 1 && chunks <= (1 << 20), NIQ_ERR_INVALID_ARG, "need 1 <= chunks <= 2^20");
+    cudaStream_t s = as_stream(stream);
+    const int grid = device_info().sm_count;
+    const size_t smem = (size_t)kTcStages * kTcStage * 4;
+    NIQ_CUDA(cudaFuncSetAttribute(k_tc_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int zero = 0;
+    NIQ_CUDA(cudaMemcpyToSymbolAsync(g_tc_rate_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+    k_tc_rate<<<grid, kTcNT, smem, s>>>(chunks < 64 ? chunks : 64, mbar_polls());   // warm-up
+    NIQ_CUDA(cudaGetLastError());
+    cudaEvent_t e0, e1;
+    NIQ_CUDA(cudaEventCreate(&e0));
+    NIQ_CUDA(cudaEventCreate(&e1));
+    NIQ_CUDA(cudaEventRecord(e0, s));
+    k_tc_rate<<<grid, kTcNT, smem, s>>>(chunks, mbar_polls());
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "k_tc_rate");
+    int st = 0;
+    NIQ_CUDA(cudaMemcpyFromSymbol(&st, g_tc_rate_status, sizeof(int)));
+    NIQ_REQUIRE(st == 0, st, "tensor-core rate probe: an MMA wait timed out");
+    const double flop = 2.0 * 128 * 256 * kTcKC * 2 * 3 * (double)chunks * grid;
+    *tflops_out = (float)(flop / (ms * 1e-3) / 1e12);
+    return NIQ_OK;
+}

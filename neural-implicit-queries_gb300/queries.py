@@ -95,11 +95,14 @@ def cast_rays_frustum(funcs_tuple, params_tuple, cam_params, in_opts):
     nev = t.zeros(1, dtype=t.int64, device='cuda')
     L = _lib.load()
     ns = int(in_opts['n_side_init'])
-    ws_bytes = L.niq_cast_frustum_workspace_size(rx, ry, ns)
+    handles = (_lib.C.c_void_p * len(models))(*[m.handle.value for m in models])
+    if bo.mode in (_lib.MODES['affine_truncate'], _lib.MODES['affine_all'], _lib.MODES['affine_append']):
+        ws_bytes = L.niq_cast_frustum_growing_workspace_size(handles, len(models), _lib.C.byref(bo), rx, ry, ns)
+    else:
+        ws_bytes = L.niq_cast_frustum_workspace_size(rx, ry, ns)
     if ws_bytes == 0:
         raise ValueError("bad resolution or n_side_init")
     ws = _io.workspace(ws_bytes)
-    handles = (_lib.C.c_void_p * len(models))(*[m.handle.value for m in models])
     co = _lib.cast_opts(in_opts)
     _lib.check(L.niq_cast_frustum(handles, len(models), _lib.C.byref(bo), _lib.C.byref(cam), _lib.C.byref(co),
                                   float(in_opts['refine_width_fac']), ns, _io.ptr(t_out), _io.ptr(hit), _io.ptr(cnt),

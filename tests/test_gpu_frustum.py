@@ -54,6 +54,29 @@ def test_frustum_matches_oracle(niq, R, gpu_ready, mode):
         assert (ref[1] > 0).sum() > 0    # the view holds surface
 
 
+@pytest.mark.parametrize('mode,kw', [('affine_truncate', {'affine_n_truncate': 8}), ('affine_all', {}),
+                                     ('affine_append', {'affine_n_append': 4})])
+def test_frustum_growing_modes_match_oracle(niq, R, gpu_ready, mode, kw):
+    """The growing-term modes: each substep's boxes go through the growing-term engine."""
+    params = niq.workloads.plain_small_model()
+    cam = camera(R, [0.3, 0.4, 2.8], 24, 20, 60., 50.)
+    opts = niq.queries.get_default_cast_opts()
+    opts['n_max_step'] = 64
+    opts['n_side_init'] = 4
+    opts['n_substeps'] = 2
+    f = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=False, **kw)[0]
+    got = niq.queries.cast_rays_frustum((f,), (params,), cam, opts)
+    ref = R.cast_rays_frustum((R.generate_implicit(params, mode, **kw),), (params,), cam, opts, trace=True)
+    assert got[0].shape == (24, 20)
+    bad = unexplained_pixels(got, ref, ref[4])
+    assert len(bad) == 0, (mode, bad[:10])
+    assert (ref[1] > 0).sum() > 0
+    # the conservative growing-term cast terminates everywhere
+    fc = niq.implicit_mlp_utils.generate_implicit_from_params(params, mode, conservative=True, **kw)[0]
+    t, hid, cnt, nev = niq.queries.cast_rays_frustum((fc,), (params,), cam, opts)
+    assert nev > 0 and np.all(np.isfinite(t)) and np.all(cnt >= 0)
+
+
 def test_frustum_two_functions_substeps(niq, R, gpu_ready):
     p1 = niq.workloads.plain_small_model()
     p2 = niq.workloads.he_mlp([3, 64, 64, 1], 'tanh', seed=5, grid=16)

@@ -109,3 +109,20 @@ def test_closest_point_node_budget(niq, gpu_ready):
                                      node_budget=8, strict=False)
     fin = np.isfinite(d)
     assert np.all(d[fin] >= full[fin] - 1e-6)
+
+
+def test_tensor_core_rate_probe_gives_up_and_recovers(niq, gpu_ready, tune):
+    """niq_tc_tf32_rate (the roofline calibration of the 3xTF32 engine): a plausible rate,
+    NIQ_ERR_TIMEOUT when its MMA waits may not poll, and a rate again afterwards."""
+    import ctypes
+    lib = niq._lib
+    L = lib.load()
+    v = ctypes.c_float(0.)
+    lib.check(L.niq_tc_tf32_rate(256, ctypes.byref(v), None))
+    assert 100. < v.value < 10000., v.value
+    tune.set_params(mbar_polls=1)
+    rc = L.niq_tc_tf32_rate(256, ctypes.byref(v), None)
+    assert rc == lib.NIQ_ERR_TIMEOUT
+    tune.set_params(mbar_polls=0)
+    lib.check(L.niq_tc_tf32_rate(256, ctypes.byref(v), None))
+    assert 100. < v.value < 10000., v.value
