@@ -79,16 +79,53 @@ def dist_info():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """SM clock and throttle reasons sampled during the timed region: NVML read through
+    ctypes every 10 ms (nvmlDeviceGetClockInfo, nvmlDeviceGetCurrentClocksEventReasons),
+    else nvidia-smi every 200 ms.  Read-only; no setting of the GPU is touched."""
     FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
               'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
               'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+    # nvmlClocksEventReason bits
+    REASONS = {0x8: 'hw_slowdown', 0x40: 'hw_thermal_slowdown', 0x20: 'sw_thermal_slowdown', 0x4: 'sw_power_cap'}
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.thread = None
+        self.rows = []
+
+    def _nvml(self):
+        import ctypes
+        try:
+            nv = ctypes.CDLL('libnvidia-ml.so.1')
+        except OSError:
+            return None
+        if nv.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.gpu), ctypes.byref(h)) != 0:
+            return None
+        return nv, h
+
+    def _poll(self, nv, h):
+        import ctypes
+        mhz, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        get_reasons = getattr(nv, 'nvmlDeviceGetCurrentClocksEventReasons', None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        while not self._stop:
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0 and get_reasons(h, ctypes.byref(rs)) == 0:
+                self.rows.append((float(mhz.value), float(mx.value), int(rs.value)))
+            time.sleep(0.01)
 
     def __enter__(self):
+        import threading
+        self._stop = False
+        handle = self._nvml()
+        if handle is not None:
+            self.thread = threading.Thread(target=self._poll, args=handle, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.gpu}', f'--query-gpu={self.FIELDS}',
                                           '--format=csv,noheader,nounits', '-lms', '200'],
@@ -99,6 +136,9 @@ class ClockSampler:
 
     def __exit__(self, *a):
         self.out = ''
+        self._stop = True
+        if self.thread is not None:
+            self.thread.join(timeout=5)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -108,6 +148,11 @@ class ClockSampler:
                 self.out, _ = self.proc.communicate()
 
     def summary(self):
+        if self.rows:
+            sm = [r[0] for r in self.rows]
+            reasons = sorted({name for r in self.rows for bit, name in self.REASONS.items() if r[2] & bit})
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(r[1] for r in self.rows),
+                    "reasons": reasons, "samples": len(self.rows), "source": "NVML, 10 ms"}
         rows = []
         for line in (self.out or '').strip().splitlines():
             p = [x.strip() for x in line.split(',')]
@@ -120,7 +165,7 @@ class ClockSampler:
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "source": "nvidia-smi, 200 ms"}
 
 
 def flush_l2(buf):
