@@ -440,6 +440,12 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models,
                               float* min_dist_out, float* min_loc_out, int64_t node_budget,
                               int32_t* status_out,
                               void* workspace, size_t workspace_bytes, void* stream);
+/* Counters of the last niq_batched_closest_point call on this workspace: the queries that
+ * stopped at node_budget (each keeps its best candidate so far, an upper bound on its
+ * distance) and the nodes bounded (a box bound and its sign samples each).  Either output
+ * may be NULL.  Read after that call's work completed; syncs `stream`. */
+int niq_batched_closest_point_stats(const void* workspace, int64_t* budget_spent_out, int64_t* nodes_out,
+                                    void* stream);
 
 /* ---- serving: continuous batching of mixed requests ---------------------------------
  * No counterpart in the reference (it has no server; its queries are called one at a

@@ -144,6 +144,7 @@ _SIGS = {
     'niq_closest_point_persistent': (C.c_int, [_P, C.POINTER(BoundOpts), _PF, _PF, _I64, _P, _F32, _I64, _P, _P, _P,
                                                _SZ, _P]),
     'niq_batched_closest_point_workspace_size': (_SZ, [_I64, _I32]),
+    'niq_batched_closest_point_stats': (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), _P]),
     'niq_batched_closest_point': (C.c_int, [C.POINTER(_P), _I32, C.POINTER(BoundOpts), _I32, C.POINTER(_I32),
                                             C.POINTER(_I64), C.POINTER(_I64), _P, _PF, _PF, _F32, _P, _P, _I64, _P,
                                             _P, _SZ, _P]),

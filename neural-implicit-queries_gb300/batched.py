@@ -75,3 +75,14 @@ def closest_point_packed(func, table, job_models, offsets, counts, query_points,
         jc.ctypes.data_as(_lib.C.POINTER(_lib.C.c_int64)), _io.ptr(q), lo, hi, float(eps), _io.ptr(dist),
         _io.ptr(loc), int(node_budget or 0), _io.ptr(status), _io.ptr(ws), ws_bytes, _io.stream_handle()))
     return dist, loc
+
+
+def stats():
+    """Counters of the last ``closest_point_packed`` call on the current device and stream:
+    ``(queries stopped at their node budget, nodes bounded)``.  A query past its budget keeps
+    its best candidate, an upper bound on its distance.  Synchronises."""
+    L = _lib.load()
+    spent, nodes = _lib.C.c_int64(0), _lib.C.c_int64(0)
+    _lib.check(L.niq_batched_closest_point_stats(_io.ptr(_io.workspace(0)), _lib.C.byref(spent), _lib.C.byref(nodes),
+                                                  _io.stream_handle()))
+    return int(spent.value), int(nodes.value)

@@ -35,6 +35,8 @@ struct BArgs {
     int interval;
     float* stacks;               // (grid * 64 slots) x kBStack x 6
     unsigned long long* next_chunk;
+    unsigned long long* n_spent;  // queries stopped at their node budget
+    unsigned long long* n_nodes;  // nodes bounded (one box bound and its samples each)
     int* err;
     int smem_floats;             // dynamic shared memory in floats
     long long node_budget;       // nodes one query may visit
@@ -111,6 +113,7 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
             // bound) and the call reports NIQ_ERR_TIMEOUT
             if (s_qid[item] >= 0 && s_top[item] > 0 && ++S.nodes[item] > a.node_budget) {
                 niq_flag_error(a.err, NIQ_ERR_TIMEOUT);
+                atomicAdd(a.n_spent, 1ull);
                 s_top[item] = 0;
                 const long long id = s_qid[item];
                 a.min_dist[id] = s_best[item];
@@ -124,7 +127,9 @@ __device__ void run_chunk(const BArgs& a, const BChunk ch, NiqSpecHeader& H, BSl
                 for (int j = 0; j < 3; ++j) { s_lo[item][j] = my_stack[6 * t + j]; s_hi[item][j] = my_stack[6 * t + 3 + j]; }
             }
         }
-        if (!__syncthreads_or(g == 0 && s_act[item])) break;
+        const int n_act = __syncthreads_count(g == 0 && s_act[item]);   // nodes bounded this round
+        if (n_act == 0) break;
+        if (threadIdx.x == 0) atomicAdd(a.n_nodes, (unsigned long long)n_act);
         const bool valid = s_act[item];
         // bound rows of the node
         {
@@ -278,6 +283,19 @@ size_t slots_max() { return (size_t)device_info().sm_count * 8 * 64; }
 
 extern "C" {
 
+int niq_batched_closest_point_stats(const void* workspace, int64_t* budget_spent_out, int64_t* nodes_out,
+                                    void* stream) {
+    NIQ_REQUIRE(workspace, NIQ_ERR_INVALID_ARG, "null workspace");
+    const char* b = reinterpret_cast<const char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    unsigned long long v[2] = {0ull, 0ull};
+    cudaStream_t s = as_stream(stream);
+    NIQ_CUDA(cudaMemcpyAsync(v, b + 16, sizeof(v), cudaMemcpyDeviceToHost, s));
+    NIQ_CUDA(cudaStreamSynchronize(s));
+    if (budget_spent_out) *budget_spent_out = (int64_t)v[0];
+    if (nodes_out) *nodes_out = (int64_t)v[1];
+    return NIQ_OK;
+}
+
 size_t niq_batched_closest_point_workspace_size(int64_t total_queries, int32_t n_jobs) {
     const size_t n_chunks = (size_t)(total_queries / kMinChunk) + (size_t)n_jobs + 1;
     return al(64) + al(n_chunks * sizeof(BChunk)) + al(n_chunks * 4) + al((size_t)(n_jobs + 1) * sizeof(NiqModelRef)) +
@@ -382,6 +400,8 @@ int niq_batched_closest_point(const niq_model* const* models, int32_t n_models, 
     a.interval = opts->mode == NIQ_MODE_INTERVAL;
     a.stacks = stacks;
     a.next_chunk = next;
+    a.n_spent = reinterpret_cast<unsigned long long*>(b + 16);   // in the header cleared above
+    a.n_nodes = reinterpret_cast<unsigned long long*>(b + 24);
     a.err = status_out ? reinterpret_cast<int*>(status_out) : err;
     a.node_budget = node_budget > 0 ? node_budget : (1ll << 62);
     a.prune_tol = eps;

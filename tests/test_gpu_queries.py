@@ -348,6 +348,33 @@ def test_batched_jobs_over_a_subset_of_a_large_table(niq, gpu_ready):
         np.testing.assert_array_equal(d_big, d_small)
 
 
+def test_batched_counts_queries_past_their_budget(niq, gpu_ready):
+    """niq_batched_closest_point_stats: the queries stopped at a node budget of one node are
+    counted, none with the default budget; each query bounds at least its root node, and no
+    more than one node under a budget of one."""
+    import torch
+    models = [niq.workloads.he_mlp([3, 32, 32, 1], 'relu', seed=70 + i, grid=8) for i in range(3)]
+    table = niq.batched.ModelTable(models)
+    f = gf(niq, models[0], conservative=True)
+    rng = np.random.default_rng(13)
+    counts = np.array([40, 25, 60], np.int64)
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    q = rng.uniform(-1.2, 1.2, (int(counts.sum()), 3)).astype(np.float32)
+    lo, hi = -np.ones(3, np.float32), np.ones(3, np.float32)
+    jm = np.arange(3, dtype=np.int32)
+    st = torch.zeros(1, dtype=torch.int32, device='cuda')
+    niq.batched.closest_point_packed(f, table, jm, offs, counts, q, lo, hi, 1e-2, status=st, node_budget=1)
+    torch.cuda.synchronize()
+    assert int(st.item()) == niq._lib.NIQ_ERR_TIMEOUT
+    spent, nodes = niq.batched.stats()
+    nq = int(counts.sum())
+    assert 0 < spent <= nq and nodes == nq
+    niq.batched.closest_point_packed(f, table, jm, offs, counts, q, lo, hi, 1e-2, status=st)
+    torch.cuda.synchronize()
+    spent, nodes = niq.batched.stats()
+    assert int(st.item()) == 0 and spent == 0 and nodes > nq
+
+
 @pytest.mark.parametrize('B', [2048, 100])
 def test_tree_schedules_agree(niq, gpu_ready, B):
     """The persistent tree, one launch per level, and the reference's schedule (launches
