@@ -90,6 +90,16 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
     }
     __syncthreads();
 
+    // WM (warp mode): one function with its weights resident -- each warp steps its own
+    // items with warp-level syncs only, refills its own slots and leaves when they are all
+    // done, so warps whose rays ended free their issue slots for the others.  (An item's
+    // threads share a warp.)  Otherwise the CTA steps in lock-step with block barriers.
+    auto run = [&](auto wm_tag) {
+    constexpr bool WM = decltype(wm_tag)::value;
+    auto sync = [&]() {
+        if constexpr (WM) __syncwarp();
+        else __syncthreads();
+    };
     while (true) {
         if (!PERSISTENT) {
             if (tile_base >= n_live) break;
@@ -105,7 +115,9 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                     for (int k = 0; k < 3; ++k) { s_root[item][k] = roots[3 * id + k]; s_dir[item][k] = dirs[3 * id + k]; }
                 }
             }
-            __syncthreads();
+            sync();
+        } else if constexpr (WM) {
+            if (!__any_sync(0xffffffffu, s_alive[item] && g == 0)) break;
         } else {
             if (!__syncthreads_or(s_alive[item] && g == 0)) break;
         }
@@ -116,7 +128,7 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                 s_act[item] = s_alive[item] && !s_hit[item];
                 s_inner[item] += s_act[item] ? 1 : 0;
             }
-            __syncthreads();
+            sync();
             for (int f = 0; f < S.n; ++f) {
                 if (S.n > 1) load_header(H, S.m[f].hdr);
                 // build rows: thread g < 4 owns input column g
@@ -149,9 +161,9 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                         }
                     }
                 }
-                __syncthreads();
+                sync();
                 const int woff = resident ? S.woff[f] : 0;
-                tile_forward<Cfg, C>(H, S.m[f].w, sW + woff, sw_cap, resident, plan, st, ob);
+                tile_forward<Cfg, C, WM>(H, S.m[f].w, sW + woff, sw_cap, resident, plan, st, ob);
                 if (g == 0 && active) {
                     const float* out = ob + item * R;
                     float lo, hi;
@@ -165,7 +177,7 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                     if (this_hit) { s_hitid[item] = f + 1; s_hit[item] = 1; }
                     atomicAdd(&s_evals[f], 1ull);
                 }
-                __syncthreads();
+                sync();
             }
             if (g == 0 && s_alive[item]) {
                 // src/queries.py:79-90
@@ -176,7 +188,7 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                 float ns = can ? __fmul_rn(sz, o.grow) : __fmul_rn(sz, o.shrink);
                 s_step[item] = fmaxf(ns, o.hit_eps);
             }
-            __syncthreads();
+            sync();
         }
         // ---- termination (src/queries.py:113-126) and slot refill
         if (g == 0 && s_alive[item]) {
@@ -202,10 +214,17 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
             const bool keep = (g == 0) && s_alive[item];
             const long long pos = niq_warp_append(&ws->n_live_next, keep);
             if (keep) live_out[pos] = (int)s_id[item];
-            __syncthreads();
+            sync();
             tile_base += (long long)gridDim.x * ITEMS;
         }
-        __syncthreads();
+        sync();
+    }
+    };
+    if constexpr (PERSISTENT) {
+        if (resident && S.n == 1) run(std::integral_constant<bool, true>());
+        else run(std::integral_constant<bool, false>());
+    } else {
+        run(std::integral_constant<bool, false>());
     }
     __syncthreads();
     if (threadIdx.x < S.n && s_evals[threadIdx.x]) atomicAdd(&n_evals[threadIdx.x], s_evals[threadIdx.x]);
