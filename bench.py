@@ -324,7 +324,8 @@ def run_ours(args):
             "form": "the reference's schedule on the same kernel: one launch per 2048 nodes, host sync per level "
                     "(niq_levelset_tree_batches)",
             "persistent_speedup": t_batch / (sum(tree_t) / len(tree_t))},
-        "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3},
+        "phases_ms": {"tree": t_tree * 1e3, "hmc": sum(hmc_t) / len(hmc_t) * 1e3,
+                      "tree_min": min(tree_t) * 1e3, "tree_max": max(tree_t) * 1e3},
         "roofline": tree_roofline(eng.value, n_boxes, bf, t_tree, params, local),
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
@@ -358,6 +359,7 @@ def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
     hidden = sum(A.shape[0] * A.shape[1] for A, _, _ in importlib.import_module(PKG).mlp.spec_layers(params)[1:-1])
     achieved = n_boxes * bf / t_tree / 1e12
     fp32_peak = fp32_peak_tflops(device)
+    fp32_nominal = fp32_nominal_tflops(device)
     tf32_peak = tf32_peak_tflops() if engine == 1 else None
     per_box = TREE_DRAM_BYTES_PER_BOX.get(engine)
     out = {"kernel": "k_tree_tc (persistent level-set tree, tensor cores)" if engine == 1
@@ -370,12 +372,11 @@ def tree_roofline(engine, n_boxes, bf, t_tree, params, device):
         out.update({"bound": "tensor", "peak": tf32_peak, "frac": achieved / tf32_peak,
                     "tensor_pipe_tflops": tensor, "tensor_pipe_frac": tensor / tf32_peak,
                     "fp32_peak": fp32_peak, "frac_of_fp32_peak": achieved / fp32_peak,
-                    "peak_source": TF32_PEAK_SOURCE + "; FP32 FMA pipe: SMs x 128 lanes x 2 FLOP x the "
-                                   "measured maximum SM clock"})
+                    "peak_source": TF32_PEAK_SOURCE + "; FP32: " + FP32_PEAK_SOURCE})
     else:
         out.update({"bound": "fp32", "peak": fp32_peak, "frac": achieved / fp32_peak,
-                    "peak_source": "FP32 FMA pipe: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock "
-                                   "(MEASURED_PEAKS.json has no FP32 figure)"})
+                    "nominal_peak": fp32_nominal, "frac_of_nominal": achieved / fp32_nominal,
+                    "peak_source": FP32_PEAK_SOURCE})
     return out
 
 
@@ -434,8 +435,10 @@ def rays_plain_method(niq, steps, warmup, l2buf):
                                 "h2d_bytes_per_step": int(roots.nbytes + dirs.nbytes),
                                 "d2h_bytes_per_step": int(t_.nbytes + hid.nbytes + cnt.nbytes + 8),
                                 "api": "queries.cast_rays (numpy in, numpy out)"}
+    nominal = fp32_nominal_tflops(torch.cuda.current_device())
     out["persistent"]["roofline"] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-                                     "frac": ach / peak, "flops_per_ray_step": 10 * macs}
+                                     "frac": ach / peak, "nominal_peak": nominal, "frac_of_nominal": ach / nominal,
+                                     "flops_per_ray_step": 10 * macs, "peak_source": FP32_PEAK_SOURCE}
     out["persistent_vs_plain"] = out["plain"]["ms_per_step"] / out["persistent"]["ms_per_step"]
     out["config"] = {"workload": "cast_rays_plain_method", "model": "relu 3-32x3-1 he-normal seed 0",
                      "rays": n, "n_max_step": 64, "mode": "affine_fixed conservative",
@@ -715,11 +718,30 @@ TF32_PEAK_SOURCE = ("tcgen05 kind::tf32 rate of the engine's dense step measured
                     "(niq_tc_tf32_rate); MEASURED_PEAKS.json has no tf32 figure")
 
 
-def fp32_peak_tflops(device=0):
-    """FP32 FMA pipe peak: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock."""
+def fp32_nominal_tflops(device=0):
+    """FP32 FMA pipe, nominal: SMs x 128 lanes x 2 FLOP x the measured maximum SM clock."""
     import torch
     sm_max = float(measured_peaks().get('sm_max_mhz', 2070.0))
     return torch.cuda.get_device_properties(device).multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+
+
+_FP32_RATE = {}
+
+
+def fp32_peak_tflops(device=0):
+    """The FP32 FMA ceiling measured live on this GPU (niq_fp32_fma_rate: packed fp32x2 FMA
+    chains on registers, every SM busy), at the clock the GPU holds now; measured once."""
+    if device not in _FP32_RATE:
+        lib = importlib.import_module(PKG + '._lib')
+        L = lib.load()
+        v = lib.C.c_float(0.)
+        lib.check(L.niq_fp32_fma_rate(8192, lib.C.byref(v), None))
+        _FP32_RATE[device] = float(v.value)
+    return _FP32_RATE[device]
+
+
+FP32_PEAK_SOURCE = ("packed fp32x2 FMA rate measured live on this GPU (niq_fp32_fma_rate); MEASURED_PEAKS.json "
+                    "has no FP32 figure; nominal = SMs x 128 lanes x 2 FLOP x the measured maximum SM clock")
 
 
 def run_precision(args):
@@ -799,7 +821,8 @@ def run_precision(args):
             row["roofline"] = {"bound": "tensor", "achieved": 3 * tf, "peak": tf32_peak, "unit": "TFLOP/s",
                                "frac": 3 * tf / tf32_peak, "peak_source": TF32_PEAK_SOURCE}
         else:
-            row["roofline"] = {"bound": "fp32", "achieved": tf, "peak": peak32, "unit": "TFLOP/s", "frac": tf / peak32}
+            row["roofline"] = {"bound": "fp32", "achieved": tf, "peak": peak32, "unit": "TFLOP/s", "frac": tf / peak32,
+                               "peak_source": FP32_PEAK_SOURCE}
         out[name] = row
     out["value"] = out["affine_truncate256_3xtf32"]["rays_per_s"]
     out["tensor_vs_fp32_classify"] = out["affine_truncate256_3xtf32"]["boxes_per_s"] / \

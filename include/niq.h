@@ -128,6 +128,12 @@ int niq_device_info(int32_t* sm_count, int32_t* max_smem_per_block);
  * with no staging and no epilogue; *tflops_out receives the measured rate in tf32
  * TFLOP/s.  Synchronises `stream`; allocates no device memory. */
 int niq_tc_tf32_rate(int32_t chunks, float* tflops_out, void* stream);
+/* The FP32 FMA ceiling of the current device (no counterpart in the reference: it
+ * calibrates the roofline of the FP32 tile engine).  Two 256-thread CTAs per SM run eight
+ * independent chains of packed fp32x2 FMAs per thread, 128 per iteration, for `iters`
+ * iterations on registers only; *tflops_out receives the measured rate in fp32 TFLOP/s
+ * (2 FLOP per FMA).  Synchronises `stream`; allocates no device memory. */
+int niq_fp32_fma_rate(int32_t iters, float* tflops_out, void* stream);
 
 /* ---- models: the dict spec of src/mlp.py:14-24,117-144 packed by the host layer ---- */
 /* Validates and uploads a packed spec (host memory) to the current device.

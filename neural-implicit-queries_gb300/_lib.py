@@ -80,6 +80,7 @@ _SIGS = {
     'niq_version': (C.c_int, []),
     'niq_device_info': (C.c_int, [C.POINTER(_I32), C.POINTER(_I32)]),
     'niq_tc_tf32_rate': (C.c_int, [_I32, _PF, _P]),
+    'niq_fp32_fma_rate': (C.c_int, [_I32, _PF, _P]),
     'niq_tune_set': (C.c_int, [_I32, _I32]),
     'niq_tune_get': (C.c_int, [_I32, C.POINTER(_I32)]),
     'niq_model_create': (C.c_int, [_P, _SZ, C.POINTER(_P)]),

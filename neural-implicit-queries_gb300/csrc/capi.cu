@@ -74,6 +74,25 @@ int validate_spec(const NiqSpecHeader& H, size_t bytes) {
     return NIQ_OK;
 }
 
+// FP32 FMA ceiling: every thread of two 256-thread CTAs per SM runs eight independent chains
+// of packed fp32x2 FMAs (the tile engine's dense instruction) on registers, no memory.
+__global__ void __launch_bounds__(256) k_fma_rate(int iters, float seed, float* sink) {
+    float2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = make_float2(seed + (float)(threadIdx.x + i), seed - (float)i);
+    const float2 m = make_float2(0.999999f, 1.000001f), c = make_float2(1e-7f, -1e-7f);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) a[i] = __ffma2_rn(a[i], m, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i].x + a[i].y;
+    if (s == 1234.5f) sink[blockIdx.x] = s;   // keeps the chains live; never true for these values
+}
+
 }  // namespace niq
 
 using namespace niq;
@@ -141,3 +160,28 @@ int niq_model_info(const niq_model* model, int32_t* max_width, int32_t* n_layers
 }
 
 }  // extern "C"
+
+extern "C" int niq_fp32_fma_rate(int32_t iters, float* tflops_out, void* stream) {
+    NIQ_REQUIRE(tflops_out && iters >= 1 && iters <= (1 << 22), NIQ_ERR_INVALID_ARG, "need 1 <= iters <= 2^22");
+    cudaStream_t s = as_stream(stream);
+    const int grid = 2 * device_info().sm_count;
+    k_fma_rate<<<grid, 256, 0, s>>>(iters < 64 ? iters : 64, 1.f, nullptr);   // warm-up
+    NIQ_CUDA(cudaGetLastError());
+    cudaEvent_t e0, e1;
+    NIQ_CUDA(cudaEventCreate(&e0));
+    NIQ_CUDA(cudaEventCreate(&e1));
+    NIQ_CUDA(cudaEventRecord(e0, s));
+    k_fma_rate<<<grid, 256, 0, s>>>(iters, 1.f, nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "k_fma_rate");
+    // 2 FMAs per packed instruction, 2 FLOP per FMA
+    const double flop = 4.0 * 8 * 16 * (double)iters * 256 * grid;
+    *tflops_out = (float)(flop / (ms * 1e-3) / 1e12);
+    return NIQ_OK;
+}

@@ -126,3 +126,20 @@ def test_tensor_core_rate_probe_gives_up_and_recovers(niq, gpu_ready, tune):
     tune.set_params(mbar_polls=0)
     lib.check(L.niq_tc_tf32_rate(256, ctypes.byref(v), None))
     assert 100. < v.value < 10000., v.value
+
+
+def test_fp32_rate_probe_is_plausible(niq, gpu_ready):
+    """niq_fp32_fma_rate (the roofline calibration of the FP32 tile engine): a rate between a
+    quarter of and the nominal FP32 FMA peak (SMs x 128 lanes x 2 FLOP x the maximum clock),
+    and bad arguments rejected."""
+    import ctypes
+    import torch
+    lib = niq._lib
+    L = lib.load()
+    v = ctypes.c_float(0.)
+    lib.check(L.niq_fp32_fma_rate(2048, ctypes.byref(v), None))
+    props = torch.cuda.get_device_properties(0)
+    nominal = props.multi_processor_count * 128 * 2 * 2.2e9 / 1e12
+    assert 0.25 * nominal < v.value < 1.05 * nominal, (v.value, nominal)
+    assert L.niq_fp32_fma_rate(0, ctypes.byref(v), None) == lib.NIQ_ERR_INVALID_ARG
+    assert L.niq_fp32_fma_rate(16, None, None) == lib.NIQ_ERR_INVALID_ARG
