@@ -6,9 +6,11 @@
 // (two M = 128 tiles), computed by tcgen05.mma kind::tf32 as three split-precision
 // products  Xhi*Ahi + Xhi*Alo + Xlo*Ahi  accumulated in fp32 in tensor memory (TMEM,
 // 512 columns: tile t at columns 256 t).  X (split on the way in) and the split weights are
-// streamed through a three-stage shared-memory ring in K chunks of 16 (weights by
-// cp.async, two chunks ahead), the MMAs issued by one
-// thread and tracked with an mbarrier per stage.  The base and err rows (one vector
+// streamed through a three-stage shared-memory ring in K chunks of 16, two chunks ahead:
+// a chunk's weights (hi and lo, contiguous in global memory) by two bulk copies of the
+// tensor memory accelerator that one thread issues, counted on the stage's "full"
+// mbarrier.  The MMAs are issued by one thread and tracked with a second mbarrier per
+// stage.  The base and err rows (one vector
 // each) are computed on the CUDA cores.
 //
 // The activation epilogue reads D straight from TMEM, thread per row:
@@ -83,13 +85,6 @@ __device__ __forceinline__ float gamma_tc(int n) {
 __device__ __forceinline__ int x_index(int r, int k) {
     return (k >> 4) * (kTcRows * kTcKC) + (int)(tc::kmajor_offset(r, k & 15, kTcKC) >> 2);
 }
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// every committed group but the most recent one complete
-__device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Column sums over a warp's 32 rows (lane = row) of 32 values per lane: lane l receives
 // the sum of column l.  The values go through the warp's own 32 x 17 shared-memory tile,
@@ -228,7 +223,8 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     float* s_newd = smem + kTcOffNew + 256;                             //                delta
     int* hist = reinterpret_cast<int*>(smem + 2048);                    // in the idle stage buffers
     __shared__ NiqSpecHeader H;
-    __shared__ __align__(8) uint64_t bar[kTcStages];
+    __shared__ __align__(8) uint64_t bar[kTcStages];    // the stage's MMAs completed
+    __shared__ __align__(8) uint64_t full[kTcStages];   // the stage's weight copies landed
     __shared__ uint32_t s_tmem;
     __shared__ float red[40];
 
@@ -236,7 +232,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     load_header(H, a.M.hdr);
     if (warp == 0) tc::tmem_alloc(&s_tmem, 512);
     if (tid == 0) {
-        for (int i = 0; i < kTcStages; ++i) tc::mbar_init(&bar[i], 1);
+        for (int i = 0; i < kTcStages; ++i) {
+            tc::mbar_init(&bar[i], 1);
+            tc::mbar_init(&full[i], 1);
+        }
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
@@ -247,6 +246,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
     // bit s of `pending` marks it, bit s of `phase` is the parity of its next completion.
     // Register bit masks, not arrays indexed by the stage, which would live in local memory.
     uint32_t pending = 0u, phase = 0u;
+    // The same for the weight copies: bit s of `fphase` is the parity of full[s]'s next
+    // completion; bit s of `fpend` (kept by the thread that issues the copies, lane 0 of warp
+    // 1, so the MMA issuer's warp is not held up by them) marks a copy in flight.
+    uint32_t fphase = 0u, fpend = 0u;
     float* xs = a.xs + (size_t)blockIdx.x * kTcXFloats;
     const int tile = warp >> 2;
     const int row = tile * 128 + (warp & 3) * 32 + lane;  // this thread's noise row
@@ -369,11 +372,15 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                     if (c < chunks && !fail) {   // no copy into a stage whose MMAs may still read it
                         const int s = c % kTcStages;
                         float* stg = smem + s * kTcStage;
-                        const int wf4 = o16 * kTcKC / 4;
-                        const float* wsrc_h = whi + (long long)c * o16 * kTcKC;
-                        const float* wsrc_l = wlo + (long long)c * o16 * kTcKC;
+                        if (tid == 32) {   // the chunk's split weights: o16 x 16 floats each, 1 KB aligned
+                            const uint32_t wbytes = (uint32_t)(o16 * kTcKC * 4);
+                            tc::mbar_arrive_expect_tx(&full[s], 2 * wbytes);
+                            tc::bulk_g2s(stg + 2 * kTcRows * kTcKC, whi + (long long)c * o16 * kTcKC, wbytes, &full[s]);
+                            tc::bulk_g2s(stg + 3 * kTcRows * kTcKC, wlo + (long long)c * o16 * kTcKC, wbytes, &full[s]);
+                            fpend |= 1u << s;
+                        }
                         const int k0 = c * kTcKC + 4 * ((tid >> 3) & 3);
-                        // X is kept once in fp32 and split here (the split weights stream with cp.async)
+                        // X is kept once in fp32 and split here
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
                             if (q >= slots) break;
@@ -394,12 +401,7 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                             *reinterpret_cast<float4*>(stg + kTcRows * kTcKC + 4 * i) =
                                 make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
                         }
-                        for (int i = tid; i < wf4; i += kTcNT) {
-                            cp_async16(stg + 2 * kTcRows * kTcKC + 4 * i, wsrc_h + 4 * i);
-                            cp_async16(stg + 3 * kTcRows * kTcKC + 4 * i, wsrc_l + 4 * i);
-                        }
                     }
-                    cp_async_commit();   // an empty group past the last chunk keeps the count
                 };
                 fetch_x(0);
                 load_chunk(0);
@@ -409,8 +411,15 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
                 for (int c = 0; c < chunks; ++c) {
                     const int s = c % kTcStages;
                     float* stg = smem + s * kTcStage;
-                    cp_async_wait_but_one();   // chunk c has landed (chunk c + 1 may be in flight)
-                    tc::fence_async_smem();
+                    if (!fail) {   // chunk c's weights have landed (chunk c + 1's may be in flight)
+                        if (tc::mbar_wait(&full[s], (fphase >> s) & 1u, a.mbar_polls)) {
+                            fphase ^= 1u << s;
+                            fpend &= ~(1u << s);
+                        } else {
+                            fail = true;
+                        }
+                    }
+                    tc::fence_async_smem();   // this thread's X stores, before the MMAs read them
                     // also: every thread is done with iteration c - 1, and all agree on `fail`
                     fail = __syncthreads_or(fail ? 1 : 0) != 0;
                     if (tid == 0 && !fail) {
@@ -647,8 +656,10 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             nrows = keep;
             n_old = n_keep_old;
             // X written by this layer visible to the next layer's copies; TMEM reads done
-            // before the next layer's MMAs overwrite it
+            // before the next layer's MMAs overwrite it; the stage buffers' use as sums and
+            // histograms ordered before the next layer's bulk copies into them
             __threadfence_block();
+            tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
@@ -706,9 +717,12 @@ __global__ void __launch_bounds__(kTcNT, 1) k_wide_tc(TcArgs a) {
             __syncthreads();   // red is rewritten by the next box
         }
     }
-    // unwind: wait (bounded) for MMAs still in flight, then free TMEM
-    for (int s = 0; s < kTcStages; ++s)
+    // unwind: wait (bounded) for MMAs and weight copies still in flight, then free TMEM
+    for (int s = 0; s < kTcStages; ++s) {
         if (!wait_stage(s, kMbarPollsDefault) && tid == 0) niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
+        if (((fpend >> s) & 1u) && !tc::mbar_wait(&full[s], (fphase >> s) & 1u, kMbarPollsDefault))
+            niq_flag_error(a.status, NIQ_ERR_TIMEOUT);
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {

@@ -50,6 +50,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
     return false;
 }
 
+// Arrives once on the mbarrier and adds `bytes` to the transaction count its current phase
+// waits for.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(
+                     smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// ---- bulk copies (TMA, untiled) -------------------------------------------------------
+// Global -> shared copy by the tensor memory accelerator: both addresses 16-byte aligned,
+// `bytes` a multiple of 16; the bytes are counted as transactions on the mbarrier.  The
+// CTA's own shared-memory address is valid in the cluster window of a non-cluster launch.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // ---- tensor memory ------------------------------------------------------------------
 // Allocation and release are warp-wide (.sync.aligned): call from one full warp.
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
