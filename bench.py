@@ -655,6 +655,17 @@ def run_rays(args):
     opts['n_max_step'] = 64
     look, up, _ = niq.render.look_at(np.array([0., 0., 3.], np.float32))
     out = {"metric": "rays/s (cast_rays, 3x32x3 ReLU MLP, affine_fixed)", "unit": "rays/s", "config": {}}
+    if args.quick:   # profiling runs: the persistent 128^2 cast only
+        roots, dirs = niq.render.generate_camera_rays(np.array([0., 0., 3.], np.float32), look, up, res=128, fov_deg=60.)
+        rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
+        dm = niq.mlp.device_model(params)
+        for _ in range(args.warmup + args.steps):
+            r = niq.queries.cast_rays((f,), (dm,), rt, dt, opts, return_device=True)
+        torch.cuda.synchronize()
+        c = r[2].cpu().numpy()
+        print(json.dumps({"quick": True, "rays": int(c.size), "ray_steps": int(c.sum()), "max_steps": int(c.max()),
+                          "steps_hist_by_8": np.bincount(np.minimum(c, 64) // 8).tolist()}))
+        return
     for res in (128, 1024):
         roots, dirs = niq.render.generate_camera_rays(np.array([0., 0., 3.], np.float32), look, up, res=res, fov_deg=60.)
         rt, dt = torch.from_numpy(roots).cuda(), torch.from_numpy(dirs).cuda()
