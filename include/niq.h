@@ -117,6 +117,12 @@ int niq_version(void);
  * waits for its MMAs with the built-in limit before it releases tensor memory). */
 #define NIQ_TUNE_BARRIER_POLLS        3
 #define NIQ_TUNE_MBAR_POLLS           4
+/* Output columns per thread of the per-ray cast's tile (niq_cast_rays and
+ * niq_cast_rays_plain in interval, affine_fixed and slope_interval): 8, or 4 (the narrow
+ * tile: twice the lanes per ray, each with half the work, for models at most 32 wide).
+ * 0 = the built-in choice: 4 for models at most 32 wide in slope_interval, or when the
+ * cast has at most 512 rays per SM.  Results are identical either way. */
+#define NIQ_TUNE_RAY_COLUMNS          5
 int niq_tune_set(int32_t param, int32_t value);
 int niq_tune_get(int32_t param, int32_t* value);
 /* Number of SMs and resident-CTA counts of the current device (for workspace sizing). */

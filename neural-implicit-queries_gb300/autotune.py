@@ -21,7 +21,9 @@ from . import _io, _lib
 
 PARAMS = {'batched_chunk': 0, 'batched_ctas_per_sm': 1, 'tree_ctas_per_sm': 2,
           # 1 + the polls a bounded device wait may make (0: built-in limit, 1: give up at once)
-          'barrier_polls': 3, 'mbar_polls': 4}
+          'barrier_polls': 3, 'mbar_polls': 4,
+          # output columns per thread of the per-ray cast (4 or 8)
+          'ray_columns': 5}
 CACHE = os.environ.get('NIQ_AUTOTUNE_CACHE', os.path.join(os.path.dirname(__file__), 'niq.autotune.json'))
 
 

@@ -108,6 +108,8 @@ int niq_tune_set(int32_t param, int32_t value) {
     NIQ_REQUIRE(value >= 0, NIQ_ERR_INVALID_ARG, "tuning values are >= 0 (0: built-in choice)");
     NIQ_REQUIRE(param != kTuneBatchedChunk || value == 0 || (value >= 32 && value <= 4096), NIQ_ERR_INVALID_ARG,
                 "batched chunk must be in [32, 4096]");
+    NIQ_REQUIRE(param != kTuneRayColumns || value == 0 || value == 4 || value == 8, NIQ_ERR_INVALID_ARG,
+                "ray-cast columns per thread must be 4 or 8 (0: built-in choice)");
     g_tune[param].store(value);
     return NIQ_OK;
 }

@@ -29,7 +29,7 @@ struct RayWs {                      // device workspace header
     int pad;
 };
 
-template <int TPI, bool C, bool SLOPE, bool PERSISTENT>
+template <int TPI, int COLS, bool C, bool SLOPE, bool PERSISTENT>
 __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, long long n, const float* __restrict__ roots,
                                                const float* __restrict__ dirs, CastDev o, float* __restrict__ t_out,
                                                int* __restrict__ hit_out, int* __restrict__ count_out,
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(kNT) k_rays(ModelSet S, int mode_interval, lon
                                                int* __restrict__ st_count, const int* __restrict__ live_in,
                                                long long n_live, int* __restrict__ live_out,
                                                int fixed_floats, int sw_cap, int resident) {
-    using Cfg = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT>, TileCfg<5, 1, TPI, kNT>>::type;
+    using Cfg = typename std::conditional<SLOPE, TileCfg<8, 4, TPI, kNT, COLS>, TileCfg<5, 1, TPI, kNT, COLS>>::type;
     constexpr int ITEMS = Cfg::ITEMS, R = Cfg::R, LD = Cfg::LD;
     extern __shared__ float4 smem4[];
     float* smem = reinterpret_cast<float*>(smem4);
@@ -477,10 +477,20 @@ int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts*
     const bool slope = mode == NIQ_MODE_SLOPE_INTERVAL;
     const int interval = mode == NIQ_MODE_INTERVAL;
     const int tpi = tpi_for_width(maxw);
+    // The narrow tile (4 columns per thread, 8 lanes per ray; same results) for models at
+    // most 32 wide: in slope_interval always (its 8-column tile needs more than 128
+    // registers and fits one CTA per SM: 1.9x faster at 128^2 and 1024^2 rays on the
+    // 3->32x3->1 model), otherwise when the rays are few enough that the cast is bound by
+    // its slowest rays' step latency rather than by throughput (up to 512 rays per SM,
+    // about four resident waves of the 8-column tile: 1.37x faster at 128^2; at 1024^2
+    // the 8-column tile is 2% faster).  The tuning parameter overrides the choice.
+    const int cols_tuned = tune_value(kTuneRayColumns);
+    const bool few = n <= 512ll * device_info().sm_count;
+    const bool narrow = maxw <= 32 && (cols_tuned == 4 || (cols_tuned == 0 && (slope || few)));
     rc = NIQ_OK;
-    auto run = [&](auto kern, int R, int TPIv) -> int {
+    auto run = [&](auto kern, int R, int TPIv, int COLSv) -> int {
         const int items = kNT / TPIv;
-        const int state = items * R * (TPIv * 8 + 4) + ((items * R + 3) & ~3);
+        const int state = items * R * (TPIv * COLSv + 4) + ((items * R + 3) & ~3);
         SmemPlan p = plan_smem(state, wfloats, maxlayer, smem_budget(kern, kNT));
         NIQ_REQUIRE(p.resident || p.sw_cap >= 5 * maxw, NIQ_ERR_UNSUPPORTED, "shared memory too small for width %d", maxw);
         int r2 = prepare_kernel(kern, p.bytes);
@@ -520,8 +530,9 @@ int launch_rays(const niq_model* const* models, int nfunc, const niq_bound_opts*
         }
         return NIQ_OK;
     };
-#define NIQ_RAYS(CC, SL)                                                           \
-    NIQ_DISPATCH_TPI(tpi, { rc = run(k_rays<TPI, CC, SL, PERSISTENT>, SL ? 8 : 5, TPI); })
+#define NIQ_RAYS(CC, SL)                                                                    \
+    if (narrow) rc = run(k_rays<8, 4, CC, SL, PERSISTENT>, SL ? 8 : 5, 8, 4);                   \
+    else NIQ_DISPATCH_TPI(tpi, { rc = run(k_rays<TPI, 8, CC, SL, PERSISTENT>, SL ? 8 : 5, TPI, 8); })
     if (slope) { if (cons) { NIQ_RAYS(true, true); } else { NIQ_RAYS(false, true); } }
     else { if (cons) { NIQ_RAYS(true, false); } else { NIQ_RAYS(false, false); } }
 #undef NIQ_RAYS

@@ -13,7 +13,7 @@ void set_error(const char* fmt, ...);
 // Launch parameters an autotuner may set (niq_tune_set); 0 means the built-in choice.
 enum TuneParam : int {
     kTuneBatchedChunk = 0, kTuneBatchedCtasPerSm = 1, kTuneTreeCtasPerSm = 2, kTuneBarrierPolls = 3,
-    kTuneMbarPolls = 4, kTuneCount = 5
+    kTuneMbarPolls = 4, kTuneRayColumns = 5, kTuneCount = 6
 };
 int tune_value(int param);
 // Poll limits of the bounded device-side waits: the tuned value minus one, or the

@@ -2,7 +2,8 @@
 //
 // One CTA holds ITEMS items; each item is R rows of width <= W (the widest layer) kept
 // in shared memory for the whole forward pass, so every layer reads its input from
-// on-chip memory.  A thread owns one item and COLS=8 output columns of every row, so
+// on-chip memory.  A thread owns one item and COLS output columns of every row (8; 4 in
+// the narrow tile, which gives an item twice the lanes and each lane half the work), so
 // the per-column range rules (radius, linearisation, rounding terms) run in registers.
 //
 // Row layouts (template R rows, the last NABS rows multiply |A| instead of A):
@@ -47,19 +48,23 @@ struct RowPlan {
 #define NIQ_FN_REL 4.76837158203125e-07f
 #define NIQ_FN_ABS 1.0e-37f
 
-template <int R_, int NABS_, int TPI_, int NT_>
+template <int R_, int NABS_, int TPI_, int NT_, int COLS_ = 8>
 struct TileCfg {
     static constexpr int R = R_;
     static constexpr int NABS = NABS_;
     static constexpr int TPI = TPI_;          // threads per item
     static constexpr int NT = NT_;            // threads per CTA
-    static constexpr int COLS = 8;            // columns per thread
+    static constexpr int COLS = COLS_;        // columns per thread
     static constexpr int NQ = COLS / 4;       // float4 groups per thread
     static constexpr int W = TPI * COLS;      // widest layer this tile supports
     static constexpr int LD = W + 4;          // row stride in floats (bank spread)
     static constexpr int ITEMS = NT / TPI;
     static constexpr int STATE_FLOATS = ITEMS * R * LD;
+    // k-slices of a single-group layer (the width-1 output layer): the narrow tile splits
+    // k as the 8-column tile with half its lanes does, so both give the same sums
+    static constexpr int KSPLIT = COLS == 4 ? (TPI > 1 ? TPI / 2 : 1) : TPI;
     static_assert(NT % TPI == 0, "tile");
+    static_assert(COLS == 4 || COLS == 8, "columns per thread");
 };
 
 // Column of float4 group q, lane j for thread g of an item: groups interleave across
@@ -352,7 +357,8 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                 A = sW;
             }
             const int kg = L.in_pad >> 2;                       // k groups of 4
-            const int per = (kg + TPI - 1) / TPI;
+            constexpr int KS = Cfg::KSPLIT;                     // lanes g >= KS get no slice
+            const int per = (kg + KS - 1) / KS;
             const int kb = min(kg, g * per), ke = min(kg, kb + per);
             for (int k4 = kb; k4 < ke; ++k4) {
                 const int k = 4 * k4;
@@ -372,7 +378,8 @@ __device__ void tile_forward(const NiqSpecHeader& H, const float* __restrict__ g
                     }
                 }
             }
-            // reduce over the item's lanes (TPI consecutive lanes of one warp)
+            // reduce over the item's lanes (TPI consecutive lanes of one warp); in the narrow
+            // tile the first step adds the empty slices' zeros, exactly
 #pragma unroll
             for (int off = TPI / 2; off > 0; off >>= 1)
 #pragma unroll

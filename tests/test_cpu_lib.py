@@ -138,11 +138,14 @@ def test_tuning_parameters_roundtrip(niq):
     at = niq.autotune
     old = at.get_params()
     try:
-        at.set_params(batched_chunk=64, batched_ctas_per_sm=1, tree_ctas_per_sm=2, barrier_polls=5, mbar_polls=1)
+        at.set_params(batched_chunk=64, batched_ctas_per_sm=1, tree_ctas_per_sm=2, barrier_polls=5, mbar_polls=1,
+                      ray_columns=8)
         assert at.get_params() == {'batched_chunk': 64, 'batched_ctas_per_sm': 1, 'tree_ctas_per_sm': 2,
-                                   'barrier_polls': 5, 'mbar_polls': 1}
+                                   'barrier_polls': 5, 'mbar_polls': 1, 'ray_columns': 8}
         with pytest.raises(ValueError):
             at.set_params(batched_chunk=7)
+        with pytest.raises(ValueError):
+            at.set_params(ray_columns=6)
         with pytest.raises(ValueError):
             at.set_params(tree_ctas_per_sm=-1)
     finally:

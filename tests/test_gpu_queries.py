@@ -89,6 +89,39 @@ def test_cast_rays_plain_method_full_size(niq, R, gpu_ready):
         assert bad.size == 0, (persistent, bad[:20])
 
 
+@pytest.mark.parametrize('mode', ['affine_fixed', 'interval', 'slope_interval'])
+@pytest.mark.parametrize('conservative', [False, True])
+def test_ray_tile_columns_agree(niq, gpu_ready, mode, conservative):
+    """The narrow ray tile (4 columns per thread, 8 lanes per ray; the default for models
+    at most 32 wide) and the 8-column tile give identical casts, persistent and plain."""
+    at = niq.autotune
+    old = at.get_params()
+    try:
+        for width in (16, 32):
+            params = niq.workloads.he_mlp([3, width, width, width, 1], 'relu', seed=40 + width, grid=16)
+            eye = np.array([0., 0., 3.], np.float32)
+            look, up, _ = niq.render.look_at(eye)
+            roots, dirs = niq.render.generate_camera_rays(eye, look, up, res=40, fov_deg=60.)
+            opts = niq.queries.get_default_cast_opts()
+            opts['n_max_step'] = 64
+            f = gf(niq, params, mode, conservative=conservative)
+            res = {}
+            for cols in (8, 4):
+                at.set_params(ray_columns=cols)
+                for persistent in (True, False):
+                    res[cols, persistent] = niq.queries.cast_rays((f,), (params,), roots, dirs, opts,
+                                                                  persistent=persistent)[:3]
+            ref = res[8, True]
+            assert int(ref[2].sum()) > 0
+            if mode != 'interval':   # interval bounds of this model are too loose to reach a hit
+                assert (ref[1] > 0).sum() > 100
+            for key, r in res.items():
+                for a, b in zip(r, ref):
+                    np.testing.assert_array_equal(a, b, err_msg=str((width, key)))
+    finally:
+        at.set_params(**old)
+
+
 @pytest.mark.parametrize('mode,kw', [('affine_all', {}), ('affine_truncate', {'affine_n_truncate': 8}),
                                      ('affine_append', {'affine_n_append': 4})])
 def test_cast_rays_growing_modes(niq, R, gpu_ready, mode, kw):
