@@ -211,6 +211,29 @@ def test_tree_oracle_spheres(niq, R, gpu_ready, conservative):
         assert len(bad) == 0, bad
 
 
+@pytest.mark.parametrize('conservative', [False, True])
+def test_tree_oracle_spheres_slope(niq, R, gpu_ready, conservative):
+    """slope_interval trees of the 12-sphere model against the oracle's: the node sets
+    agree except boxes that a near decision on their path explains; outward rounding may
+    keep more boxes unknown, and drops one only where such a decision explains it."""
+    params = niq.workloads.spheres_sdf_model()
+    f = gf(niq, params, 'slope_interval', conservative=conservative)
+    d = niq.kd_tree.construct_uniform_unknown_levelset_tree(f, params, -np.ones(3), np.ones(3), split_depth=12)
+    o = R.generate_implicit(params, 'slope_interval')
+    r = R.construct_uniform_unknown_levelset_tree(o, params, -np.ones(3), np.ones(3), split_depth=12)
+    n_ref = len(r['unknown_node_lower'])
+    assert n_ref > 100
+    extra, missing = box_set_diff(d['unknown_node_lower'], d['unknown_node_upper'], r['unknown_node_lower'],
+                                  r['unknown_node_upper'])
+    if conservative:
+        assert len(extra) <= 0.01 * n_ref + 2, (len(extra), n_ref)
+        bad = unexplained_boxes(params, missing, -np.ones(3), np.ones(3), mode='slope_interval')
+    else:
+        bad = unexplained_boxes(params, np.concatenate([extra, missing]), -np.ones(3), np.ones(3),
+                                mode='slope_interval')
+    assert len(bad) == 0, bad
+
+
 def test_hmc_oracle_and_golden(niq, R, gpu_ready):
     from oracle import mc_table
     g = golden('tree.npz')
