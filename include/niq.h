@@ -316,8 +316,8 @@ int niq_levelset_tree_plain(const niq_model* model, const niq_bound_opts* opts,
  * - Results go to the caller's arrays, each (NIQ_STATIC_TREE_NODES, 3) float32 (interior
  *   and exterior only when requested in flags); counts_out as for niq_levelset_tree.
  * - The first call on a device looks up the scratch array's device address and keeps it
- *   for the process; make that first call before any stream capture, and make no call
- *   after a cudaDeviceReset of that device.  Every call clears the counters it needs.
+ *   for the process; make no call after a cudaDeviceReset of that device.  Every call
+ *   clears the counters it needs.
  * - All calls share the one scratch array: calls that overlap on the GPU (two streams,
  *   or two host threads) race and corrupt each other's results.  Syncs the stream. */
 #define NIQ_STATIC_TREE_NODES 65536
