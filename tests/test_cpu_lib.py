@@ -32,6 +32,34 @@ def test_library_exports_every_header_function(lib):
     assert set(names) == set(L.exported_symbols())
 
 
+def test_c_abi_checks_arguments_before_device_work(lib, niq):
+    """The C ABI's argument and spec checks return their status before any device work,
+    so they hold on a machine without a GPU: bad counts, null pointers, and packed specs
+    whose header does not validate (src/mlp.py:131,142), each with a message."""
+    import ctypes
+    L, so = lib
+    v = ctypes.c_float(0.)
+    assert so.niq_fp32_fma_rate(0, ctypes.byref(v), None) == L.NIQ_ERR_INVALID_ARG
+    assert b'iters' in so.niq_last_error()
+    assert so.niq_tc_tf32_rate(0, ctypes.byref(v), None) == L.NIQ_ERR_INVALID_ARG
+    assert b'chunks' in so.niq_last_error()
+    out = ctypes.c_void_p()
+    assert so.niq_model_create(None, 0, ctypes.byref(out)) == L.NIQ_ERR_INVALID_ARG
+    blob = bytes(niq.mlp.pack(niq.workloads.he_mlp([3, 8, 1], 'relu', seed=1, grid=8)))
+    buf = ctypes.create_string_buffer(blob[:16], 16)
+    assert so.niq_model_create(buf, 16, ctypes.byref(out)) == L.NIQ_ERR_BAD_SPEC
+    assert b'too short' in so.niq_last_error()
+    bad = bytearray(blob)
+    bad[0] ^= 0xFF                                   # magic
+    buf = ctypes.create_string_buffer(bytes(bad), len(bad))
+    assert so.niq_model_create(buf, len(bad), ctypes.byref(out)) == L.NIQ_ERR_BAD_SPEC
+    assert b'magic' in so.niq_last_error()
+    buf = ctypes.create_string_buffer(blob, len(blob))
+    assert so.niq_model_create(buf, len(blob) - 4, ctypes.byref(out)) == L.NIQ_ERR_BAD_SPEC
+    assert b'does not match' in so.niq_last_error()
+    assert out.value is None
+
+
 def test_mc_table_library_matches_oracle(lib):
     from oracle import mc_table
     L, so = lib
