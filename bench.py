@@ -298,8 +298,31 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - t0)
     t_e2e = sum(e2e_times) / len(e2e_times)
 
+    # ---- the CPU reference arm's work: the same tree and marching cubes in the reference's
+    #      arithmetic (no outward rounding), end to end through the same call
+    f_ref, _ = niq.implicit_mlp_utils.generate_implicit_from_params(params, 'affine_fixed', conservative=False)
+    bo_ref = f_ref.bound_opts()
+    lib.check(L.niq_levelset_tree(model.handle, lib.C.byref(bo_ref), lo3, hi3, args.split_depth, 0, 0.0, 0, cap,
+                                  io.ptr(counts), io.ptr(ws), ws_bytes, stream.cuda_stream))
+    n_boxes_ref = int(counts.cpu().numpy()[3])
+
+    def e2e_ref_step():
+        return kd.hierarchical_marching_cubes(f_ref, params, lower, upper, args.split_depth // 3, n_subcell_depth=0)
+    for _ in range(args.warmup):
+        out_ref = e2e_ref_step()
+    torch.cuda.synchronize()
+    ref_times = []
+    for _ in range(max(3, args.steps // 2)):
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_ref = e2e_ref_step()
+        torch.cuda.synchronize()
+        ref_times.append(time.perf_counter() - t0)
+    t_e2e_ref = sum(ref_times) / len(ref_times)
+
     # ---- max over ranks
-    t_step, t_e2e, t_plain, t_batch = max_over_ranks([t_step, t_e2e, t_plain, t_batch], world)
+    t_step, t_e2e, t_plain, t_batch, t_e2e_ref = max_over_ranks([t_step, t_e2e, t_plain, t_batch, t_e2e_ref], world)
     value = replica_rate(n_boxes, t_step, world)
     bf = box_flops(params)
     t_tree = sum(tree_t) / len(tree_t)
@@ -316,6 +339,11 @@ def run_ours(args):
         "e2e": {"value": replica_rate(n_boxes, t_e2e, world), "unit": "boxes/s", "h2d_bytes_per_step": 24,
                 "d2h_bytes_per_step": int(out.nbytes) + 32, "ms_per_step": t_e2e * 1e3,
                 "api": "kd_tree.hierarchical_marching_cubes(depth=8, n_subcell_depth=0)"},
+        "e2e_reference_arithmetic": {
+            "value": replica_rate(n_boxes_ref, t_e2e_ref, world), "unit": "boxes/s", "ms_per_step": t_e2e_ref * 1e3,
+            "boxes_per_step": n_boxes_ref, "triangles_per_step": int(len(out_ref)),
+            "api": "kd_tree.hierarchical_marching_cubes(depth=8, n_subcell_depth=0), conservative=False",
+            "note": "the work of the CPU reference arm: the tree and marching cubes without outward rounding"},
         "plain": {"value": replica_rate(n_boxes, t_plain, world), "unit": "boxes/s", "ms_per_step": t_plain * 1e3,
                   "form": "one launch + host sync per level (niq_levelset_tree_plain)",
                   "persistent_speedup": t_plain / (sum(tree_t) / len(tree_t))},
