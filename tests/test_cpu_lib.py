@@ -161,6 +161,26 @@ def test_generate_implicit_modes(niq):
         niq.affine.AffineContext('nope')
 
 
+def test_autotune_cache_roundtrip(niq, tmp_path, monkeypatch):
+    """The autotuner's cache on the host: a stored choice is found again by its key and
+    applied through niq_tune_set; unknown keys and a corrupt file give no choice."""
+    at = niq.autotune
+    old = at.get_params()
+    monkeypatch.setattr(at, 'CACHE', str(tmp_path / 'tune.json'))
+    try:
+        assert at.apply('batched|none') is None
+        at._store('batched|k1', {'batched_chunk': 256, 'batched_ctas_per_sm': 1})
+        at._store('tree|k2', {'tree_ctas_per_sm': 2})
+        assert at.apply('batched|k1') == {'batched_chunk': 256, 'batched_ctas_per_sm': 1}
+        p = at.get_params()
+        assert p['batched_chunk'] == 256 and p['batched_ctas_per_sm'] == 1
+        assert at.apply('tree|k2') == {'tree_ctas_per_sm': 2} and at.get_params()['tree_ctas_per_sm'] == 2
+        (tmp_path / 'tune.json').write_text('{not json')
+        assert at.apply('batched|k1') is None
+    finally:
+        at.set_params(**old)
+
+
 def test_tuning_parameters_roundtrip(niq):
     """niq_tune_set/get on the host (no device work): values stick, bad ones are refused."""
     at = niq.autotune
