@@ -41,3 +41,21 @@ def test_box_flops_of_the_default_workload(niq):
     params = niq.workloads.spheres_sdf_model()
     assert bench.mlp_macs(params) == 12544
     assert bench.box_flops(params) == 125440
+
+
+def test_reference_arm_line():
+    """`bench.py --impl reference` (the oracle's C/OpenMP tree and marching cubes on the
+    host cores) prints one JSON line with the keys the benchmark contract names, for the
+    24-bisection tree of the 12-sphere model: 3,677,207 boxes and 264,040 triangles in the
+    reference's arithmetic, the counts the GPU's tree gives without outward rounding."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--steps', '1',
+                        '--warmup', '0'], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d['impl'] == 'reference' and d['unit'] == 'boxes/s' and d['higher_is_better'] is True
+    assert d['value'] > 0 and d['steps'] == 1
+    assert d['details']['boxes_per_step'] == 3677207 and d['details']['triangles_per_step'] == 264040
+    assert d['cpu_baseline']['kind'] == 'port' and d['cpu_baseline']['value'] == d['value']
+    assert d['e2e'] == {"value": d['value'], "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
